@@ -1,0 +1,397 @@
+"""Benchmark: FDK voxel-view updates/s on one GB300, plain FP32 vs BF16-storage form.
+
+Workload (one step = one full fdk(plan, proj): view weights + ramp filter + cone-beam
+back-projection): CtFanFlat ns=512, nt=384, ds=dt=1, dsd=1000, dso=600, na=720 over 360
+deg; ImageGeom 512x512x256 at 0.5 mm; projections of 30 seeded random ellipsoids
+(centres in the cylinder r<=100, |z|<=50, semi-axes U[3,60], ZYZ Euler angles, density
+U[-0.3,1]) computed on the GPU.  One step is 512*512*256*720 = 48.3e9 voxel-view
+updates.  Inputs (566 MB of projections) are larger than L2 (129 MB).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU (torchrun): every rank reconstructs its own scan (independent replicas,
+weak scaling, no collective on the data path); the timed region is bracketed by a
+barrier and the max time over ranks is reported.  `--impl reference` times the
+reference algorithm's CPU restatement (the oracle port; the Julia reference cannot run
+here) on the host cores for the same workload, sampled by z-slab.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sinograms.jl_gb300"))
+
+WORKLOAD = "fdk_ctfanflat_512x512x256_from_512x384x720"
+GEOM = dict(ns=512, nt=384, ds=1.0, dt=1.0, dsd=1000.0, dod=400.0, na=720, orbit=360.0)
+IMG = dict(dims=(512, 512, 256), deltas=(0.5, 0.5, 0.5))
+METRIC = "FDK voxel-view updates/s: plain FP32 vs BF16 form at <=1e-4 rel RMSE vs FP64"
+UNIT = "voxel-view updates/s"
+F_UPD = 15  # FP32 flops per voxel-view update counted for the compute roofline
+NOMINAL_FP32_TFLOPS = 152 * 128 * 2 * 2.070e9 / 1e12  # 152 SMs x 128 lanes x FMA x max clock
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _phantom():
+    import sinograms as S
+    return S.random_ellipsoids(30, 3, 100.0, 50.0, axes=(3.0, 60.0), dens=(-0.3, 1.0))
+
+
+def _oracle_geom():
+    return dict(kind="flat", offset_s=0.0, offset_t=0.0, orbit_start=0.0, source_offset=0.0, **GEOM)
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _traffic_from_profile(name: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
+    (a line 'traffic_bytes_per_launch: N'), or None."""
+    p = os.path.join(ROOT, "profiles", name)
+    try:
+        for line in open(p):
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except Exception:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index):
+        self.proc = None
+        try:
+            import torch
+            uuid = str(torch.cuda.get_device_properties(dev_index).uuid)
+            sel = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+        except Exception:
+            sel = str(dev_index)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100", "-i", sel], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        time.sleep(0.15)
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            return None
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import sinograms as S
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if ws > 1:
+            dist.barrier()
+
+    rg = S.CtFanFlat(**GEOM)
+    ig = S.ImageGeom(IMG["dims"], IMG["deltas"])
+    nvox = int(np.prod(IMG["dims"]))
+    upd = nvox * rg.na
+    proj = S.ellipsoid_proj(rg, _phantom(), device=True)  # each rank: its own scan
+    st = torch.cuda.current_stream()
+    forms = {}
+    outs = {}
+    for storage in ("f32", "bf16"):
+        plan = S.plan_fbp(rg, ig, storage=storage)
+        plan.set_timing(True)
+        img = torch.empty(tuple(reversed(IMG["dims"])), dtype=torch.float32, device="cuda")
+        for _ in range(args.warmup):
+            S.fdk(plan, proj, out=img, sync=False)
+        torch.cuda.synchronize()
+        barrier()
+        sampler = ClockSampler(local)
+        l0 = S.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        fms, bms = [], []
+        for _ in range(args.steps):
+            S.fdk(plan, proj, out=img, sync=False)
+            f_ms, b_ms = plan.last_timing()
+            fms.append(f_ms)
+            bms.append(b_ms)
+        e1.record(st)
+        torch.cuda.synchronize()
+        launches = S.launch_count() - l0
+        clocks = sampler.stop()
+        barrier()
+        ms = e0.elapsed_time(e1)
+        if ws > 1:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        forms[storage] = dict(ms_per_step=ms / args.steps, value=ws * upd * args.steps / (ms / 1e3),
+                              filter_ms=float(np.mean(fms)), back_ms=float(np.mean(bms)), gpu_launches=launches,
+                              clocks=clocks, plan=plan)
+        outs[storage] = img
+    head = "bf16"
+    # e2e through the public API with pinned host buffers (H2D of the projections and
+    # D2H of the volume inside the timed region, every step)
+    plan = forms[head]["plan"]
+    hproj = torch.empty(proj.shape, dtype=torch.float32, pin_memory=True)
+    hproj.copy_(proj)
+    himg = torch.empty(tuple(reversed(IMG["dims"])), dtype=torch.float32, pin_memory=True)
+    hp, hi = hproj.numpy(), himg.numpy()
+    S.fdk(plan, hp, out=hi)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        S.fdk(plan, hp, out=hi)  # blocking call: copies in, computes, copies out
+    e2e_s = time.perf_counter() - t0
+    if ws > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    barrier()
+
+    peaks = _peaks()
+    hbm = peaks.get("hbm_gbs")
+    f = forms[head]
+    alg_bytes = proj.numel() * (2 if head == "bf16" else 4) + nvox * 4  # read filtered proj + write volume
+    achieved = alg_bytes / (f["back_ms"] / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": f["value"], "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: 30 seeded random ellipsoids, analytic cone-beam "
+        "projections generated on the GPU",
+        "config": {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5,
+                   "storage": "bf16 filtered projections, fp32 arithmetic", "updates_per_step": upd,
+                   "l2": "inputs larger than L2 (566 MB projections per step)", "parallelism": f"replicas x{ws}"},
+        "forms": {k: {"value": v["value"], "ms_per_step": v["ms_per_step"], "filter_ms": v["filter_ms"],
+                      "back_ms": v["back_ms"]} for k, v in forms.items()},
+        "e2e": {"value": ws * upd * args.steps / e2e_s, "unit": UNIT,
+                "h2d_bytes_per_step": proj.numel() * 4, "d2h_bytes_per_step": nvox * 4},
+        "roofline": {"bound": "hbm", "kernel": "fdk_back_kernel", "achieved": achieved, "peak": hbm,
+                     "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
+                     "alg_bytes_per_launch": alg_bytes,
+                     "traffic": _traffic_from_profile("fdk_back_kernel_config3.md"),
+                     "fp32_issue": {"flops_per_update": F_UPD,
+                                    "achieved_tflops": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12,
+                                    "peak_tflops_nominal": NOMINAL_FP32_TFLOPS,
+                                    "frac": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12 / NOMINAL_FP32_TFLOPS}},
+        "gpu_launches": f["gpu_launches"],
+        "clocks": f["clocks"],
+    }
+    if ws == 1 and rank == 0 and not args.no_cpu:
+        base, acc = cpu_leg({k: v.cpu().numpy() for k, v in outs.items()}, proj.cpu().numpy())
+        line["cpu_baseline"] = base
+        line["accuracy_vs_fp64"] = acc
+        if acc["bf16"]["rel_rmse"] > 1e-4:  # headline form must meet the accuracy bound
+            line["value"] = forms["f32"]["value"]
+            line["config"]["storage"] = "fp32 (bf16 form exceeded 1e-4 rel RMSE)"
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------- CPU side
+
+def _slab_rows(rg, z_lo, z_hi, rxy):
+    """Detector rows (0-based, inclusive) that voxels with z in [z_lo, z_hi] and
+    radius <= rxy can reach: t' = mag * z with mag in [dsd/(dso+rxy), dsd/(dso-rxy)]."""
+    dso = rg["dsd"] - rg["dod"]
+    mags = (rg["dsd"] / (dso + rxy), rg["dsd"] / (dso - rxy))
+    ts = [m * z / rg["dt"] for m in mags for z in (z_lo, z_hi)]
+    wt = (rg["nt"] + 1) / 2
+    lo = max(0, int(math.floor(min(ts) + wt)) - 2 - 1)
+    hi = min(rg["nt"] - 1, int(math.floor(max(ts) + wt)) + 2)
+    return lo, hi
+
+
+def cpu_fdk_slab(O, proj, rg, z_idx, threads, bits=32):
+    """Reference algorithm on the CPU for the voxels in z-slices z_idx: weight, FFT ramp
+    filter of the detector rows those voxels reach, back-projection. Returns
+    (image_slab, seconds, updates)."""
+    ax = O.image_axes(dict(dims=IMG["dims"], deltas=IMG["deltas"]))
+    zc = ax[2][z_idx]
+    rxy = math.hypot(abs(ax[0]).max(), abs(ax[1]).max())
+    lo, hi = _slab_rows(rg, zc.min(), zc.max(), rxy)
+    dt_ = np.float32 if bits == 32 else np.float64
+    t0 = time.perf_counter()
+    w = O.fdk_weights(rg)[:, lo:hi + 1, :].astype(dt_)
+    band = proj[:, lo:hi + 1, :].astype(dt_) * w
+    Hk = O.fbp_filter(rg)
+    filt = np.zeros(proj.shape, dtype=dt_)
+    filt[:, lo:hi + 1, :] = O.sino_filter_fft(band, Hk, workers=threads)
+    img = _back_z(O, filt, rg, ax, zc, bits)
+    sec = time.perf_counter() - t0
+    return img, sec, IMG["dims"][0] * IMG["dims"][1] * len(z_idx) * rg["na"]
+
+
+def _back_z(O, filt, rg, ax, zc, bits, xs=None, ys=None):
+    import ctypes
+    L = O.lib(bits)
+    xc = np.ascontiguousarray(ax[0] if xs is None else ax[0][xs])
+    yc = np.ascontiguousarray(ax[1] if ys is None else ax[1][ys])
+    zc = np.ascontiguousarray(zc)
+    na, nt, ns = filt.shape
+    img = np.zeros((len(zc), len(yc), len(xc)), dtype=filt.dtype)
+    b = np.ascontiguousarray(O.ar(rg))
+    rc = L.orc_cbct_back(ctypes.c_void_p(img.ctypes.data), ctypes.c_void_p(filt.ctypes.data), ns, nt, na,
+                         ctypes.c_void_p(b.ctypes.data), ctypes.c_double(rg["dsd"]), ctypes.c_double(O.dso(rg)),
+                         ctypes.c_double(rg["ds"]), ctypes.c_double(rg["dt"]), ctypes.c_float(0.0),
+                         ctypes.c_float(0.0), 0, ctypes.c_void_p(xc.ctypes.data), ctypes.c_void_p(yc.ctypes.data),
+                         ctypes.c_void_p(zc.ctypes.data), len(xc), len(yc), len(zc), None, 1)
+    assert rc == 0
+    return img
+
+
+def _threads():
+    return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+
+
+def cpu_leg(gpu_imgs, proj):
+    """CPU baseline (FP32 restatement of the reference loops, all host threads) on a
+    central z-slab, and FP64 accuracy of both GPU forms on a sparse voxel sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    rg = _oracle_geom()
+    th = _threads()
+    nz = IMG["dims"][2]
+    # calibrate on 2 slices, then size the slab for ~10 s of CPU work
+    _, sec, u = cpu_fdk_slab(O, proj, rg, np.arange(nz // 2 - 1, nz // 2 + 1), th)
+    k = int(min(64, max(4, 2 * 10.0 / max(sec, 1e-3))))
+    z_idx = np.arange(nz // 2 - k // 2, nz // 2 - k // 2 + k)
+    _, sec, u = cpu_fdk_slab(O, proj, rg, z_idx, th)
+    base = {"value": u / sec, "unit": UNIT, "cores": th, "kind": "port",
+            "sample": f"fdk of the central {k}-slice z-slab (512x512x{k} voxels x 720 views = {u:.3g} updates): "
+                      f"weights + FFT ramp filter of the detector rows the slab reaches + FP32 back-projection "
+                      f"(oracle restatement of the reference loops; Julia is not available here)",
+            "seconds": sec}
+    # FP64 accuracy on a sparse sample: every 16th x/y voxel, 8 z-slices spread over z
+    xs, ys = np.arange(0, 512, 16), np.arange(0, 512, 16)
+    zs = np.linspace(0, nz - 1, 8).round().astype(int)
+    filt = O.sino_filter_fft(proj.astype(np.float64) * O.fdk_weights(rg), O.fbp_filter(rg), workers=th)
+    ax = O.image_axes(dict(dims=IMG["dims"], deltas=IMG["deltas"]))
+    ref = _back_z(O, filt, rg, ax, ax[2][zs], 64, xs, ys)
+    acc = {}
+    for k_, img in gpu_imgs.items():
+        sub = img[np.ix_(zs, ys, xs)]
+        acc[k_] = {"rel_rmse": O.rel_rmse(sub, ref),
+                   "max_abs_err_rel": float(np.abs(sub - ref).max() / np.abs(ref).max()),
+                   "sample": "32x32x8 voxels (every 16th x,y; 8 z-slices), FP64 oracle"}
+    return base, acc
+
+
+def run_reference(args):
+    """Reference arm: the reference algorithm on the host cores (oracle FP32 port), same
+    metric and workload; each step is a bounded z-slab sample."""
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    import sinograms as S
+    rg = _oracle_geom()
+    th = _threads()
+    # projections of the same phantom (GPU generator if present, else the oracle's)
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError
+        proj = S.ellipsoid_proj(S.CtFanFlat(**GEOM), _phantom(), device=True).cpu().numpy()
+    except Exception:
+        proj = O.ellipsoid_proj(rg, _phantom()).astype(np.float32)
+    nz = IMG["dims"][2]
+    k = 8
+    slabs = [np.arange(z0, z0 + k) for z0 in range(0, nz, k)]
+    for i in range(args.warmup):
+        cpu_fdk_slab(O, proj, rg, slabs[i % len(slabs)], th)
+    tot_s, tot_u = 0.0, 0
+    for i in range(args.steps):
+        _, sec, u = cpu_fdk_slab(O, proj, rg, slabs[(args.warmup + i * 5) % len(slabs)], th)
+        tot_s += sec
+        tot_u += u
+    v = tot_u / tot_s
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "impl": "reference",
+            "data": "synthetic: 30 seeded random ellipsoids (same phantom as the GPU arm)",
+            "config": {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                             "sample": f"each step: fdk of one {k}-slice z-slab (512x512x{k} x 720 views): weights + "
+                                       "FFT ramp filter of the rows it reaches + FP32 back-projection; oracle "
+                                       "restatement of the reference (Julia not available)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

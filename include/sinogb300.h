@@ -1,0 +1,210 @@
+/*
+ * sinogb300.h -- C ABI of libsinogb300.so, the GB300 (sm_103a) implementation of the
+ * Sinograms.jl reconstruction hot path.
+ *
+ * Each entry point names the reference function it replaces (file:line, paths relative
+ * to the Sinograms.jl v0.5.1 project root).  The library never throws across the ABI:
+ * every call returns an int status (SGB_OK == 0) and sgb_last_error() gives the
+ * message of the calling thread's last failure.
+ *
+ * Array layout is Julia's column-major order (first index fastest), so Julia arrays
+ * pass straight through `ccall`:
+ *   projections (ns, nt, na), sinograms (nb, na), images (nx, ny[, nz]);
+ *   the distance-driven pair uses the reference's own layouts: phantom (nPix, nPix)
+ *   with row = y (row 1 at the top) and sinogram (na, nDet).
+ * Bulk arrays are host pointers unless `flags` has SGB_DEVICE_PTRS, in which case they
+ * are device pointers on the current CUDA device.  Geometry vectors (angles, sin/cos
+ * tables, pixel-centre axes, filter responses) are always small host arrays.
+ * `stream` is a cudaStream_t (NULL = legacy default stream).  Calls block until the
+ * result is complete unless flags has SGB_ASYNC (device pointers only).
+ */
+#ifndef SINOGB300_H
+#define SINOGB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SGB_API __attribute__((visibility("default")))
+#else
+#define SGB_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SGB_OK 0
+#define SGB_ERR_ARG 1         /* bad size / argument: reference throw("...") or error() */
+#define SGB_ERR_CUDA 2        /* CUDA runtime failure */
+#define SGB_ERR_NOMEM 3       /* device allocation failed */
+#define SGB_ERR_GEOM 4        /* impossible geometry (ramp.jl:217-219) */
+#define SGB_ERR_UNSUPPORTED 5 /* combination the reference also rejects */
+#define SGB_ERR_TIMEOUT 6     /* a bounded device-side wait gave up */
+
+/* flags */
+#define SGB_DEVICE_PTRS 1 /* bulk arrays are device pointers */
+#define SGB_ASYNC 2       /* do not synchronize the stream before returning */
+
+/* geometry kinds: SinoPar, SinoFanArc/CtFanArc, SinoFanFlat/CtFanFlat */
+#define SGB_PAR 0
+#define SGB_ARC 1
+#define SGB_FLAT 2
+
+/* window shapes, window.jl:317-329 and WindowVect :279 */
+#define SGB_WIN_NONE 0
+#define SGB_WIN_BOXCAR 1
+#define SGB_WIN_HAMMING 2
+#define SGB_WIN_HANN 3
+#define SGB_WIN_VECT 4
+
+/* storage of the filtered projections inside fdk/fbp */
+#define SGB_STORE_F32 0
+#define SGB_STORE_BF16 1
+
+/* SinoPar / SinoFanArc / SinoFanFlat fields, src/geom/type2.jl:95-159 */
+typedef struct {
+    int kind;             /* SGB_PAR, SGB_ARC, SGB_FLAT */
+    int nb;
+    double d;
+    float offset;         /* Toffset = Float32, src/geom/util.jl:5 */
+    int na;
+    double orbit;         /* degrees */
+    double orbit_start;   /* degrees */
+    double source_offset; /* fan only */
+    double dsd;           /* fan only */
+    double dod;           /* fan only */
+} sgb_sino_geom;
+
+/* CtFanArc / CtFanFlat fields, src/geom/type3.jl:145-184 (circular source) */
+typedef struct {
+    int kind; /* SGB_ARC or SGB_FLAT */
+    int ns, nt;
+    double ds, dt;
+    float offset_s, offset_t;
+    int na;
+    double orbit, orbit_start;
+    double source_offset, dsd, dod;
+} sgb_ct_geom;
+
+/* ImageGeom (ImageGeoms.jl 0.11): centres x_i = delta*(i - (n+1)/2 - offset). */
+typedef struct {
+    int ndim;             /* 2 or 3 */
+    int dims[3];
+    double deltas[3];
+    double offsets[3];
+    const uint8_t *mask;  /* host, dims-shaped, nonzero = reconstruct; NULL = all true */
+} sgb_image_geom;
+
+/* plan_fbp keyword options, plan2.jl:106-117 / plan3.jl:60-68 */
+typedef struct {
+    int window_shape;          /* SGB_WIN_* */
+    double cutoff;             /* Window cutoff (default 1) */
+    const double *window_vect; /* SGB_WIN_VECT only, length npad */
+    int npad;                  /* 0 = nextpow(2, n + 1) */
+    int decon1;                /* default 1 */
+    const double *filter;      /* optional user Hk of length npad (overrides the above) */
+    int storage;               /* SGB_STORE_F32 or SGB_STORE_BF16 */
+} sgb_filter_opts;
+
+typedef struct sgb_plan sgb_plan;
+
+/* ----------------------------------------------------------------- library */
+SGB_API int sgb_version(void);
+/* Copies the calling thread's last error message (NUL terminated, truncated to n). */
+SGB_API int sgb_last_error(char *buf, size_t n);
+/* Number of CUDA kernels this library has launched since load (all threads). */
+SGB_API long long sgb_launch_count(void);
+
+/* -------------------------------------------------- plan-time (host, FP64) */
+/* fbp_ramp / ramp_flat / ramp_arc, src/fbp/ramp.jl:171-238; kind SGB_PAR|SGB_FLAT = flat. */
+SGB_API int sgb_fbp_ramp(int kind, int N, double ds, double dsd, double *h);
+/* fbp_window, src/fbp/window.jl:298-312 (fftshift'ed, Float32-valued) */
+SGB_API int sgb_fbp_window(int shape, double cutoff, int N, const double *vect, double *win);
+/* fbp_filter, src/fbp/filter.jl:32-57 */
+SGB_API int sgb_fbp_filter(int kind, int npad, double ds, double dsd, int shape, double cutoff,
+                   const double *vect, int decon1, double *Hk);
+/* _angle_weights, src/fbp/d-angle.jl:55-65 */
+SGB_API int sgb_angle_weight(const double *ar, int na, double *w);
+/* parker_weight(::SinoGeom), src/fbp/parker.jl:58 and :111-119.  w has room for
+ * nb*na values; *n0,*n1 receive the Julia dims written: (1,1), (1,na) or (nb,na). */
+SGB_API int sgb_parker_weight_sino(const sgb_sino_geom *rg, float *w, int *n0, int *n1);
+/* parker_weight(::CtFan), src/fbp/parker.jl:147-154.  w: ns*na; *n0,*n2 get (1,1) or (ns,na). */
+SGB_API int sgb_parker_weight_ct(const sgb_ct_geom *rg, float *w, int *n0, int *n2);
+/* fdk_weight_cyl, src/fbp3/fdk.jl:21-45 -> w (ns, nt) */
+SGB_API int sgb_fdk_weight_cyl(const sgb_ct_geom *rg, double *w);
+/* fbp_sino_weight, src/fbp2/sino-weight.jl:12-16 -> w (nb) */
+SGB_API int sgb_fbp_sino_weight(const sgb_sino_geom *rg, double *w);
+
+/* ------------------------------------------------------------ GPU kernels */
+/* fbp_sino_filter, src/fbp/filter.jl:122-147: in (nb, nrows) -> out (nb+extra, nrows). */
+SGB_API int sgb_fbp_sino_filter(const float *in, int nb, long long nrows, const double *Hk, int npad,
+                        int extra, float *out, int flags, void *stream);
+
+/* cbct_back_fan!, src/fbp3/cbct-back.jl:95-144 (with cbct_back_fan_voxel :150-213).
+ * betas: na source angles (radians); views 1:ia_skip:na are used.  mask may be NULL. */
+SGB_API int sgb_cbct_back(float *image, const float *proj, int ns, int nt, int na, const double *betas,
+                  double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
+                  int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
+                  int nz, const uint8_t *mask, int ia_skip, int flags, void *stream);
+
+/* fbp_back_par!, src/fbp2/back-par.jl:360-407 (with fbp_back_par_xy :430-469).
+ * sino (nb, na); sinphi/cosphi hold the ceil(na/ia_skip) views 1:ia_skip:na. */
+SGB_API int sgb_fbp_back_par(float *image, const float *sino, int nb, int na, const double *sinphi,
+                     const double *cosphi, double ds, float offset, const double *xc,
+                     const double *yc, int nx, int ny, const uint8_t *mask, int ia_skip, int flags,
+                     void *stream);
+
+/* fbp_back_fan!, src/fbp2/back-fan.jl:215-254 (with fbp_back_fan_xy :280-336). */
+SGB_API int sgb_fbp_back_fan(float *image, const float *sino, int nb, int na, const double *sinb,
+                     const double *cosb, double dsd, double dso, double source_offset, int is_arc,
+                     double ds, float offset, const double *xc, const double *yc, int nx, int ny,
+                     const uint8_t *mask, int ia_skip, int flags, void *stream);
+
+/* project_bdd, src/sys2/bdd_2d.jl:17-110: phantom (nPix,nPix) -> sino (na, nDet). */
+SGB_API int sgb_bdd_project(const float *phantom, int nPix, int nDet, int na, const double *angle,
+                    double DSD, double DS0, double pSize, double dSize, float *sino, int flags,
+                    void *stream);
+/* backproject_bdd, src/sys2/bdd_2d.jl:119-220: sino (na, nDet) -> image (nPix,nPix). */
+SGB_API int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const double *angle,
+                        double DSD, double DS0, double pSize, double dSize, float *image, int flags,
+                        void *stream);
+
+/* Analytic line integrals standing in for ImagePhantoms.radon(rays(rg), ob) in the
+ * reference tests (test/fbp2/fbp-fan.jl:106-109, test/fbp3/fdk.jl:23), with the ray
+ * geometry of rays(rg) (sino-geom.jl:368-401, ct-geom.jl:227-239).
+ * ell rows: 2D (cx, cy, rx, ry, angle, density); 3D (cx, cy, cz, rx, ry, rz, phi, theta,
+ * psi, density) with ZYZ Euler angles.  Output: sino (nb, na) / proj (ns, nt, na). */
+SGB_API int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nell, float *sino, int flags,
+                     void *stream);
+SGB_API int sgb_ellipsoid_proj(const sgb_ct_geom *rg, const double *ell, int nell, float *proj, int flags,
+                       void *stream);
+
+/* ------------------------------------------------------------------ plans */
+/* plan_fbp(rg::CtGeom, ig), src/fbp3/plan3.jl:60-72 (FDKplan). */
+SGB_API int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
+                    sgb_plan **plan);
+/* plan_fbp(rg::SinoGeom, ig), src/fbp2/plan2.jl:106-138 (FBPNormalPlan). */
+SGB_API int sgb_plan_fbp_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig,
+                      const sgb_filter_opts *opt, sgb_plan **plan);
+/* plan.filter (Hk, length npad) and the dims of plan.view_weight. */
+SGB_API int sgb_plan_filter(const sgb_plan *plan, double *Hk, int *npad);
+/* fdk(plan, proj), src/fbp3/fdk.jl:65-81: proj (ns,nt,na) -> image (nx,ny,nz). */
+SGB_API int sgb_fdk(sgb_plan *plan, const float *proj, float *image, int flags, void *stream);
+/* fbp(plan, sino) for one 2D sinogram or a stack, src/fbp2/fbp.jl:24-68:
+ * sino (nb, na, nslices) -> image (nx, ny, nslices). */
+SGB_API int sgb_fbp(sgb_plan *plan, const float *sino, float *image, int nslices, int flags,
+            void *stream);
+SGB_API int sgb_plan_destroy(sgb_plan *plan);
+/* Stage timing (no counterpart in the reference): when enabled, fdk/fbp record CUDA
+ * events on the call's stream around the filter and back-projection kernels;
+ * sgb_plan_last_timing waits for them and returns ms[0] = weighted filter,
+ * ms[1] = back-projection of the last call. */
+SGB_API int sgb_plan_set_timing(sgb_plan *plan, int enable);
+SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SINOGB300_H */

@@ -181,14 +181,14 @@ int orc_sino_filter(const real_t *in, int nb, long nrows, const double *Hk, int 
 
 /* --------------------------------------------------------------- d-angle.jl */
 
-/* _angle_weights, src/fbp/d-angle.jl:55-65 (scalar |da| / n180). */
-int orc_angle_weight(const double *ar, int na, double *w) {
+/* _angle_weights, src/fbp/d-angle.jl:55-65 (scalar |da| / n180).  rtol is isapprox's
+ * default sqrt(eps(T)) of the angles' element type (d-angle.jl:57). */
+int orc_angle_weight_tol(const double *ar, int na, double rtol, double *w) {
     if (na < 2) return ORC_ERR_ARG;
     double da0 = ar[1] - ar[0];
     for (int i = 1; i < na - 1; i++) {
         double da = ar[i + 1] - ar[i];
-        /* isapprox with default rtol = sqrt(eps) (d-angle.jl:57) */
-        if (fabs(da - da0) > 1.4901161193847656e-08 * fmax(fabs(da), fabs(da0))) return ORC_ERR_ARG;
+        if (fabs(da - da0) > rtol * fmax(fabs(da), fabs(da0))) return ORC_ERR_ARG;
     }
     double last = ar[na - 1] - ar[na - 2];
     double next = ar[na - 1] + last;
@@ -197,6 +197,10 @@ int orc_angle_weight(const double *ar, int na, double *w) {
     if (n180 < 1) n180 = 1;
     *w = fabs(da0 / n180);
     return ORC_OK;
+}
+
+int orc_angle_weight(const double *ar, int na, double *w) {
+    return orc_angle_weight_tol(ar, na, 1.4901161193847656e-08, w); /* sqrt(eps(Float64)) */
 }
 
 /* ---------------------------------------------------------------- parker.jl */

@@ -380,3 +380,20 @@ def ellipsoid_proj(rg, ell) -> np.ndarray:
 def rel_rmse(x, ref) -> float:
     x, ref = np.asarray(x, np.float64), np.asarray(ref, np.float64)
     return float(np.linalg.norm(x - ref) / np.linalg.norm(ref))
+
+
+def sino_filter_fft(x: np.ndarray, Hk: np.ndarray, workers: int = 1, chunk_rows: int = 1 << 16) -> np.ndarray:
+    """fbp_sino_filter with the reference's own FFT formulation (filter.jl:122-147:
+    zero-pad to npad, fft, multiply by Hk, ifft, real part, crop), on the last axis.
+    float32 input is transformed in complex64 like FFTW on Float32 data."""
+    import scipy.fft as sfft
+    npad, nb = len(Hk), x.shape[-1]
+    flat = x.reshape(-1, nb)
+    out = np.empty_like(flat)
+    H = Hk.astype(np.float32 if flat.dtype == np.float32 else np.float64)
+    for r0 in range(0, flat.shape[0], chunk_rows):
+        blk = flat[r0:r0 + chunk_rows]
+        F = sfft.fft(blk, n=npad, axis=-1, workers=workers)
+        F *= H
+        out[r0:r0 + chunk_rows] = sfft.ifft(F, axis=-1, workers=workers).real[:, :nb]
+    return out.reshape(x.shape)

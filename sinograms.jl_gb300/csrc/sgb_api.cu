@@ -1,0 +1,640 @@
+// sgb_api.cu -- extern "C" entry points of libsinogb300.so (declared in include/sinogb300.h):
+// plans (plan_fbp / fdk / fbp) and the per-kernel seams the reference's mutating
+// functions map onto.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "sgb_common.cuh"
+#include "sgb_host.h"
+#include "sgb_kernels.cuh"
+
+using namespace sgb;
+
+namespace {
+
+cudaStream_t as_stream(void *s) { return static_cast<cudaStream_t>(s); }
+
+// pixel centres of one ImageGeom axis divided by ds: delta*(i - (n-1)/2 - offset)/ds
+std::vector<double> image_axis(int n, double delta, double offset, double ds) {
+    std::vector<double> v(n);
+    for (int i = 0; i < n; i++) v[i] = delta * (i - ((n - 1) / 2.0 + offset)) / ds;
+    return v;
+}
+
+int upload_f64(const double *src, size_t n, DevBuf &dst, cudaStream_t st) {
+    SGB_TRY(dst.reserve(n * sizeof(double)));
+    SGB_CUDA(cudaMemcpyAsync(dst.p, src, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int upload_raw(const void *src, size_t bytes, DevBuf &dst, cudaStream_t st) {
+    SGB_TRY(dst.reserve(bytes));
+    SGB_CUDA(cudaMemcpyAsync(dst.p, src, bytes, cudaMemcpyHostToDevice, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+// device copy of a host mask, or null when the mask is absent or all true
+int upload_mask(const uint8_t *mask, size_t n, DevBuf &dst, const uint8_t **dev, cudaStream_t st) {
+    *dev = nullptr;
+    if (!mask) return SGB_OK;
+    bool all = true;
+    for (size_t i = 0; i < n && all; i++) all = mask[i] != 0;
+    if (all) return SGB_OK;
+    SGB_TRY(upload_raw(mask, n, dst, st));
+    *dev = dst.as<uint8_t>();
+    return SGB_OK;
+}
+
+// view trig table (FP64 sincos on the device) for the used views 1:ia_skip:na
+int make_trig(const double *betas, int na, int ia_skip, DevBuf &bet, DevBuf &trig, cudaStream_t st) {
+    SGB_TRY(upload_f64(betas, na, bet, st));
+    int nv = (na + ia_skip - 1) / ia_skip;
+    SGB_TRY(trig.reserve(sizeof(float2) * nv));
+    return launch_view_trig(bet.as<double>(), na, ia_skip, trig.as<float2>(), st);
+}
+
+int trig_from_sincos(const double *sn, const double *cs, int nv, DevBuf &trig, cudaStream_t st) {
+    std::vector<float2> h(nv);
+    for (int i = 0; i < nv; i++) h[i] = make_float2((float)sn[i], (float)cs[i]);
+    return upload_raw(h.data(), sizeof(float2) * nv, trig, st);
+}
+
+}  // namespace
+
+struct sgb_plan {
+    bool ct = false;
+    sgb_ct_geom cg{};
+    sgb_sino_geom sg{};
+    int nx = 0, ny = 0, nz = 1;
+    int storage = SGB_STORE_F32;
+    int npad = 0;
+    std::vector<double> Hk;
+    int ndet = 0, nrow = 1, na = 0;  // ns|nb, nt|1, na
+    // device tables
+    DevBuf gext, wA, wB, trig, betas, xds, yds, zds, mask;
+    const uint8_t *mask_dev = nullptr;
+    long long sAj = 0, sAa = 0, sBj = 0, sBt = 0;
+    bool hasA = false, hasB = false;
+    float scale = 1.f;
+    // staging for host-pointer calls
+    DevBuf in_buf, filt_buf, img_buf;
+    // optional stage timing
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    ~sgb_plan() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    void mark(int i, cudaStream_t st) {
+        if (timing) cudaEventRecord(ev[i], st);
+    }
+};
+
+namespace {
+
+int plan_common(sgb_plan *P, int kind, int ndet, double d, double dsd, const sgb_filter_opts *opt,
+                int nrow, int na, const double *ar, cudaStream_t st) {
+    sgb_filter_opts o{};
+    o.cutoff = 1.0;
+    o.decon1 = 1;
+    if (opt) o = *opt;
+    P->storage = o.storage;
+    P->ndet = ndet;
+    P->nrow = nrow;
+    P->na = na;
+    P->npad = o.npad > 0 ? o.npad : next_pow2(ndet + 1);  // nextpow(2, n+1)
+    SGB_REQUIRE(P->npad >= ndet, "nb=%d + extra=0 > npad=%d", ndet, P->npad);
+    if (o.filter) {
+        P->Hk.assign(o.filter, o.filter + P->npad);
+    } else {
+        SGB_TRY(filter_response(kind == SGB_ARC ? SGB_ARC : SGB_FLAT, P->npad, d, dsd, o.window_shape,
+                                o.cutoff == 0 ? 1.0 : o.cutoff, o.window_vect, o.decon1, P->Hk));
+    }
+    std::vector<double> g;
+    spatial_kernel(P->Hk, g);
+    std::vector<float> gx;
+    build_gext(g, ndet, gx);
+    SGB_TRY(upload_raw(gx.data(), gx.size() * sizeof(float), P->gext, st));
+    double w;
+    SGB_TRY(angle_weight(ar, na, &w));
+    P->scale = (float)w;
+    SGB_TRY(make_trig(ar, na, 1, P->betas, P->trig, st));
+    return SGB_OK;
+}
+
+int plan_image(sgb_plan *P, const sgb_image_geom *ig, double ds, int ndim, cudaStream_t st) {
+    SGB_REQUIRE(ig && ig->ndim == ndim, "ImageGeom must be %dD", ndim);
+    P->nx = ig->dims[0];
+    P->ny = ig->dims[1];
+    P->nz = ndim == 3 ? ig->dims[2] : 1;
+    SGB_REQUIRE(P->nx > 0 && P->ny > 0 && P->nz > 0, "image dims must be positive");
+    std::vector<double> x = image_axis(P->nx, ig->deltas[0], ig->offsets[0], ds);
+    std::vector<double> y = image_axis(P->ny, ig->deltas[1], ig->offsets[1], ds);
+    SGB_TRY(upload_f32(x.data(), x.size(), 1.0, P->xds, st));
+    SGB_TRY(upload_f32(y.data(), y.size(), 1.0, P->yds, st));
+    if (ndim == 3) {
+        std::vector<double> z = image_axis(P->nz, ig->deltas[2], ig->offsets[2], ds);
+        SGB_TRY(upload_f32(z.data(), z.size(), 1.0, P->zds, st));
+    }
+    return upload_mask(ig->mask, (size_t)P->nx * P->ny * P->nz, P->mask, &P->mask_dev, st);
+}
+
+}  // namespace
+
+extern "C" {
+
+// ----------------------------------------------------------------------- plans
+
+int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
+                    sgb_plan **plan) {
+    SGB_REQUIRE(rg && ig && plan, "plan_fbp: null argument");
+    SGB_REQUIRE(rg->kind == SGB_ARC || rg->kind == SGB_FLAT, "plan_fbp: CtGeom must be CtFanArc or CtFanFlat");
+    SGB_REQUIRE(rg->ns > 1 && rg->nt > 1 && rg->na > 1, "plan_fbp: ns, nt, na must exceed 1");
+    cudaStream_t st = 0;
+    sgb_plan *P = new sgb_plan();
+    P->ct = true;
+    P->cg = *rg;
+    std::vector<double> ar = view_angles(rg->na, rg->orbit, rg->orbit_start);
+    int s = plan_common(P, rg->kind, rg->ns, rg->ds, rg->dsd, opt, rg->nt, rg->na, ar.data(), st);
+    if (s == SGB_OK) s = plan_image(P, ig, rg->ds, 3, st);
+    if (s == SGB_OK) {  // _fdk_weights = parker .* fdk_weight_cyl .* dbeta (plan3.jl:75-80)
+        std::vector<float> pk((size_t)rg->ns * rg->na);
+        int n0, n2;
+        s = sgb_parker_weight_ct(rg, pk.data(), &n0, &n2);
+        if (s == SGB_OK && n0 > 1) {
+            s = upload_raw(pk.data(), pk.size() * sizeof(float), P->wA, st);
+            P->hasA = true;
+            P->sAj = 1;
+            P->sAa = rg->ns;
+        }
+        std::vector<double> cyl((size_t)rg->ns * rg->nt);
+        if (s == SGB_OK) s = sgb_fdk_weight_cyl(rg, cyl.data());
+        if (s == SGB_OK) s = upload_f32(cyl.data(), cyl.size(), 1.0, P->wB, st);
+        P->hasB = true;
+        P->sBj = 1;
+        P->sBt = rg->ns;
+    }
+    if (s != SGB_OK) {
+        delete P;
+        return s;
+    }
+    *plan = P;
+    return SGB_OK;
+}
+
+int sgb_plan_fbp_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig,
+                      const sgb_filter_opts *opt, sgb_plan **plan) {
+    SGB_REQUIRE(rg && ig && plan, "plan_fbp: null argument");
+    SGB_REQUIRE(rg->kind >= SGB_PAR && rg->kind <= SGB_FLAT, "plan_fbp: unknown SinoGeom kind");
+    SGB_REQUIRE(rg->nb > 1 && rg->na > 1, "plan_fbp: nb, na must exceed 1");
+    cudaStream_t st = 0;
+    sgb_plan *P = new sgb_plan();
+    P->sg = *rg;
+    std::vector<double> ar = view_angles(rg->na, rg->orbit, rg->orbit_start);
+    int s = plan_common(P, rg->kind, rg->nb, rg->d, rg->dsd, opt, 1, rg->na, ar.data(), st);
+    if (s == SGB_OK) s = plan_image(P, ig, rg->d, 2, st);
+    if (s == SGB_OK) {
+        // fan: fbp_sino_weight (fbp.jl:36) folded with view_weight = parker .* dbeta
+        std::vector<float> pk((size_t)rg->nb * rg->na);
+        int n0, n1;
+        s = sgb_parker_weight_sino(rg, pk.data(), &n0, &n1);
+        std::vector<double> sw(rg->nb, 1.0);
+        if (s == SGB_OK && rg->kind != SGB_PAR) s = sgb_fbp_sino_weight(rg, sw.data());
+        if (s == SGB_OK) {
+            bool fan = rg->kind != SGB_PAR;
+            if (n0 > 1) {  // (nb, na)
+                std::vector<double> a((size_t)rg->nb * rg->na);
+                for (int j = 0; j < rg->na; j++)
+                    for (int i = 0; i < rg->nb; i++)
+                        a[i + (size_t)rg->nb * j] = sw[i] * pk[i + (size_t)rg->nb * j];
+                s = upload_f32(a.data(), a.size(), 1.0, P->wA, st);
+                P->sAj = 1;
+                P->sAa = rg->nb;
+                P->hasA = true;
+            } else if (n1 > 1) {  // SinoPar with atypical orbit: (1, na)
+                std::vector<double> a(rg->na);
+                for (int j = 0; j < rg->na; j++) a[j] = pk[j];
+                s = upload_f32(a.data(), a.size(), 1.0, P->wA, st);
+                P->sAj = 0;
+                P->sAa = 1;
+                P->hasA = true;
+            } else if (fan) {
+                s = upload_f32(sw.data(), sw.size(), 1.0, P->wA, st);
+                P->sAj = 1;
+                P->sAa = 0;
+                P->hasA = true;
+            }
+        }
+    }
+    if (s != SGB_OK) {
+        delete P;
+        return s;
+    }
+    *plan = P;
+    return SGB_OK;
+}
+
+int sgb_plan_filter(const sgb_plan *plan, double *Hk, int *npad) {
+    SGB_REQUIRE(plan && npad, "plan_filter: null argument");
+    *npad = plan->npad;
+    if (Hk) memcpy(Hk, plan->Hk.data(), sizeof(double) * plan->npad);
+    return SGB_OK;
+}
+
+int sgb_plan_destroy(sgb_plan *plan) {
+    delete plan;
+    return SGB_OK;
+}
+
+int sgb_plan_set_timing(sgb_plan *P, int enable) {
+    SGB_REQUIRE(P, "plan_set_timing: null plan");
+    if (enable)
+        for (auto &e : P->ev)
+            if (!e) SGB_CUDA(cudaEventCreate(&e));
+    P->timing = enable != 0;
+    return SGB_OK;
+}
+
+int sgb_plan_last_timing(sgb_plan *P, double *ms, int n) {
+    SGB_REQUIRE(P && ms && n >= 2, "plan_last_timing: bad argument");
+    SGB_REQUIRE(P->timing, "plan_last_timing: timing is not enabled");
+    float a, b;
+    SGB_CUDA(cudaEventSynchronize(P->ev[2]));
+    SGB_CUDA(cudaEventElapsedTime(&a, P->ev[0], P->ev[1]));
+    SGB_CUDA(cudaEventElapsedTime(&b, P->ev[1], P->ev[2]));
+    ms[0] = a;
+    ms[1] = b;
+    return SGB_OK;
+}
+
+static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *out, cudaStream_t st) {
+    FilterArgs A{};
+    A.in = in_dev;
+    A.ns = P->ndet;
+    A.nout = P->ndet;
+    A.nrows = nrows;
+    A.nt = P->nrow;
+    A.na = P->na;
+    A.wA = P->hasA ? P->wA.as<float>() : nullptr;
+    A.sAj = P->sAj;
+    A.sAa = P->sAa;
+    A.wB = P->hasB ? P->wB.as<float>() : nullptr;
+    A.sBj = P->sBj;
+    A.sBt = P->sBt;
+    A.scale = P->scale;
+    A.gext = P->gext.as<float>();
+    return launch_filter_rows(A, out, P->storage == SGB_STORE_BF16, st);
+}
+
+int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *stream) {
+    SGB_REQUIRE(P && proj && image, "fdk: null argument");
+    SGB_REQUIRE(P->ct, "fdk: plan is not a CT (FDK) plan");
+    cudaStream_t st = as_stream(stream);
+    const sgb_ct_geom &g = P->cg;
+    const size_t nproj = (size_t)g.ns * g.nt * g.na, nvox = (size_t)P->nx * P->ny * P->nz;
+    const void *in_dev;
+    SGB_TRY(stage_in(proj, nproj * sizeof(float), flags, P->in_buf, &in_dev, st));
+    SGB_TRY(P->filt_buf.reserve(nproj * (P->storage == SGB_STORE_BF16 ? 2 : 4)));
+    // step 1+2: view weights fused into the ramp filter (fdk.jl:72-75)
+    P->mark(0, st);
+    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.nt * g.na, P->filt_buf.p, st));
+    P->mark(1, st);
+    float *img_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->img_buf.reserve(nvox * sizeof(float)));
+        img_dev = P->img_buf.as<float>();
+    }
+    // step 3: cbct_back (fdk.jl:78)
+    FdkArgs A{};
+    A.proj = P->filt_buf.p;
+    A.image = img_dev;
+    A.mask = P->mask_dev;
+    A.trig = P->trig.as<float2>();
+    A.xds = P->xds.as<float>();
+    A.yds = P->yds.as<float>();
+    A.zds = P->zds.as<float>();
+    A.ns = g.ns;
+    A.nt = g.nt;
+    A.na = g.na;
+    A.nx = P->nx;
+    A.ny = P->ny;
+    A.nz = P->nz;
+    A.nv = g.na;
+    A.ia_skip = 1;
+    A.ws = (float)((g.ns + 1) / 2.0 + g.offset_s);
+    A.wt = (float)((g.nt + 1) / 2.0 + g.offset_t);
+    A.dsd_ds = (float)(g.dsd / g.ds);
+    A.dso_ds = (float)((g.dsd - g.dod) / g.ds);
+    A.inv_dtds = (float)(g.ds / g.dt);
+    A.is_arc = g.kind == SGB_ARC;
+    A.bf16 = P->storage == SGB_STORE_BF16;
+    SGB_TRY(launch_fdk_back(A, st));
+    P->mark(2, st);
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return finish(flags, st);
+}
+
+int sgb_fbp(sgb_plan *P, const float *sino, float *image, int nslices, int flags, void *stream) {
+    SGB_REQUIRE(P && sino && image, "fbp: null argument");
+    SGB_REQUIRE(!P->ct, "fbp: plan is a CT plan; use fdk");
+    SGB_REQUIRE(nslices >= 1, "fbp: nslices must be >= 1");
+    SGB_REQUIRE(P->storage == SGB_STORE_F32, "fbp: 2D plans store filtered sinograms in FP32");
+    cudaStream_t st = as_stream(stream);
+    const sgb_sino_geom &g = P->sg;
+    const size_t nsino = (size_t)g.nb * g.na * nslices, npix = (size_t)P->nx * P->ny * nslices;
+    const void *in_dev;
+    SGB_TRY(stage_in(sino, nsino * sizeof(float), flags, P->in_buf, &in_dev, st));
+    SGB_TRY(P->filt_buf.reserve(nsino * sizeof(float)));
+    P->mark(0, st);
+    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.na * nslices, P->filt_buf.p, st));
+    P->mark(1, st);
+    float *img_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->img_buf.reserve(npix * sizeof(float)));
+        img_dev = P->img_buf.as<float>();
+    }
+    Back2Args A{};
+    A.sino = P->filt_buf.as<float>();
+    A.image = img_dev;
+    A.mask = P->mask_dev;
+    A.trig = P->trig.as<float2>();
+    A.xds = P->xds.as<float>();
+    A.yds = P->yds.as<float>();
+    A.nb = g.nb;
+    A.na = g.na;
+    A.nx = P->nx;
+    A.ny = P->ny;
+    A.nv = g.na;
+    A.ia_skip = 1;
+    A.nslices = nslices;
+    A.wb = (float)((g.nb + 1) / 2.0 + g.offset);
+    A.mode = g.kind;
+    A.dsd_ds = (float)(g.dsd / g.d);
+    A.dso_ds = (float)((g.dsd - g.dod) / g.d);
+    A.so_ds = (float)(g.source_offset / g.d);
+    SGB_TRY(launch_back2(A, st));
+    P->mark(2, st);
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, img_dev, npix * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return finish(flags, st);
+}
+
+// ----------------------------------------------------------------------- seams
+
+int sgb_fbp_sino_filter(const float *in, int nb, long long nrows, const double *Hk, int npad,
+                        int extra, float *out, int flags, void *stream) {
+    SGB_REQUIRE(in && out && Hk, "fbp_sino_filter: null argument");
+    SGB_REQUIRE(nb > 0 && nrows >= 0 && extra >= 0, "fbp_sino_filter: bad sizes");
+    SGB_REQUIRE(nb + extra <= npad, "nb=%d + extra=%d > npad=%d", nb, extra, npad);  // filter.jl:131
+    cudaStream_t st = as_stream(stream);
+    std::vector<double> hk(Hk, Hk + npad), g;
+    spatial_kernel(hk, g);
+    std::vector<float> gx;
+    build_gext(g, nb, gx);
+    DevBuf dg, din, dout;
+    SGB_TRY(upload_raw(gx.data(), gx.size() * sizeof(float), dg, st));
+    const void *in_dev;
+    SGB_TRY(stage_in(in, sizeof(float) * nb * (size_t)nrows, flags, din, &in_dev, st));
+    float *out_dev = out;
+    size_t out_bytes = sizeof(float) * (size_t)(nb + extra) * nrows;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dout.reserve(out_bytes));
+        out_dev = dout.as<float>();
+    }
+    FilterArgs A{};
+    A.in = static_cast<const float *>(in_dev);
+    A.ns = nb;
+    A.nout = nb + extra;
+    A.nrows = nrows;
+    A.nt = 1;
+    A.na = 1;
+    A.scale = 1.f;
+    A.gext = dg.as<float>();
+    SGB_TRY(launch_filter_rows(A, out_dev, 0, st));
+    if (!(flags & SGB_DEVICE_PTRS)) SGB_CUDA(cudaMemcpyAsync(out, out_dev, out_bytes, cudaMemcpyDeviceToHost, st));
+    return finish(flags, st);
+}
+
+int sgb_cbct_back(float *image, const float *proj, int ns, int nt, int na, const double *betas,
+                  double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
+                  int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
+                  int nz, const uint8_t *mask, int ia_skip, int flags, void *stream) {
+    SGB_REQUIRE(image && proj && betas && xc && yc && zc, "cbct_back: null argument");
+    SGB_REQUIRE(ns > 0 && nt > 0 && na > 0 && nx >= 0 && ny >= 0 && nz >= 0, "size mismatch");
+    SGB_REQUIRE(ia_skip >= 1, "cbct_back: ia_skip must be >= 1");
+    cudaStream_t st = as_stream(stream);
+    DevBuf bet, trig, dx, dy, dz, dproj, dimg, dmask;
+    SGB_TRY(make_trig(betas, na, ia_skip, bet, trig, st));
+    std::vector<double> xv(xc, xc + nx), yv(yc, yc + ny), zv(zc, zc + nz);
+    SGB_TRY(upload_f32(xv.data(), nx, 1.0 / ds, dx, st));
+    SGB_TRY(upload_f32(yv.data(), ny, 1.0 / ds, dy, st));
+    SGB_TRY(upload_f32(zv.data(), nz, 1.0 / ds, dz, st));
+    const size_t nproj = (size_t)ns * nt * na, nvox = (size_t)nx * ny * nz;
+    const void *proj_dev;
+    SGB_TRY(stage_in(proj, nproj * sizeof(float), flags, dproj, &proj_dev, st));
+    const uint8_t *mask_dev = nullptr;
+    if (mask) {
+        const void *m;
+        SGB_TRY(stage_in(mask, nvox, flags, dmask, &m, st));
+        mask_dev = static_cast<const uint8_t *>(m);
+    }
+    float *img_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dimg.reserve(nvox * sizeof(float)));
+        img_dev = dimg.as<float>();
+    }
+    FdkArgs A{};
+    A.proj = proj_dev;
+    A.image = img_dev;
+    A.mask = mask_dev;
+    A.trig = trig.as<float2>();
+    A.xds = dx.as<float>();
+    A.yds = dy.as<float>();
+    A.zds = dz.as<float>();
+    A.ns = ns;
+    A.nt = nt;
+    A.na = na;
+    A.nx = nx;
+    A.ny = ny;
+    A.nz = nz;
+    A.nv = (na + ia_skip - 1) / ia_skip;
+    A.ia_skip = ia_skip;
+    A.ws = (float)((ns + 1) / 2.0 + offset_s);  // cbct-back.jl:119-120
+    A.wt = (float)((nt + 1) / 2.0 + offset_t);
+    A.dsd_ds = (float)(dsd / ds);
+    A.dso_ds = (float)(dso / ds);
+    A.inv_dtds = (float)(ds / dt);
+    A.is_arc = is_arc != 0;
+    A.bf16 = 0;
+    SGB_TRY(launch_fdk_back(A, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));  // temporaries are released on return
+    return SGB_OK;
+}
+
+static int back2_seam(float *image, const float *sino, int nb, int na, const double *sn,
+                      const double *cs, int mode, double dsd, double dso, double source_offset,
+                      double ds, float offset, const double *xc, const double *yc, int nx, int ny,
+                      const uint8_t *mask, int ia_skip, int flags, void *stream) {
+    SGB_REQUIRE(image && sino && sn && cs && xc && yc, "fbp_back: null argument");
+    SGB_REQUIRE(nb > 0 && na > 0 && nx >= 0 && ny >= 0, "size mismatch");
+    SGB_REQUIRE(ia_skip >= 1, "fbp_back: ia_skip must be >= 1");
+    cudaStream_t st = as_stream(stream);
+    const int nv = (na + ia_skip - 1) / ia_skip;
+    DevBuf trig, dx, dy, dsino, dimg, dmask;
+    SGB_TRY(trig_from_sincos(sn, cs, nv, trig, st));
+    std::vector<double> xv(xc, xc + nx), yv(yc, yc + ny);
+    SGB_TRY(upload_f32(xv.data(), nx, 1.0 / ds, dx, st));
+    SGB_TRY(upload_f32(yv.data(), ny, 1.0 / ds, dy, st));
+    const void *sino_dev;
+    SGB_TRY(stage_in(sino, sizeof(float) * (size_t)nb * na, flags, dsino, &sino_dev, st));
+    const uint8_t *mask_dev = nullptr;
+    if (mask) {
+        const void *m;
+        SGB_TRY(stage_in(mask, (size_t)nx * ny, flags, dmask, &m, st));
+        mask_dev = static_cast<const uint8_t *>(m);
+    }
+    float *img_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dimg.reserve(sizeof(float) * (size_t)nx * ny));
+        img_dev = dimg.as<float>();
+    }
+    Back2Args A{};
+    A.sino = static_cast<const float *>(sino_dev);
+    A.image = img_dev;
+    A.mask = mask_dev;
+    A.trig = trig.as<float2>();
+    A.xds = dx.as<float>();
+    A.yds = dy.as<float>();
+    A.nb = nb;
+    A.na = na;
+    A.nx = nx;
+    A.ny = ny;
+    A.nv = nv;
+    A.ia_skip = ia_skip;
+    A.nslices = 1;
+    A.wb = (float)((nb + 1) / 2.0 + offset);  // back-par.jl:378, back-fan.jl:236
+    A.mode = mode;
+    A.dsd_ds = (float)(dsd / ds);
+    A.dso_ds = (float)(dso / ds);
+    A.so_ds = (float)(source_offset / ds);
+    SGB_TRY(launch_back2(A, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, img_dev, sizeof(float) * (size_t)nx * ny, cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));  // temporaries are released on return
+    return SGB_OK;
+}
+
+int sgb_fbp_back_par(float *image, const float *sino, int nb, int na, const double *sinphi,
+                     const double *cosphi, double ds, float offset, const double *xc,
+                     const double *yc, int nx, int ny, const uint8_t *mask, int ia_skip, int flags,
+                     void *stream) {
+    return back2_seam(image, sino, nb, na, sinphi, cosphi, SGB_PAR, 0, 0, 0, ds, offset, xc, yc, nx,
+                      ny, mask, ia_skip, flags, stream);
+}
+
+int sgb_fbp_back_fan(float *image, const float *sino, int nb, int na, const double *sinb,
+                     const double *cosb, double dsd, double dso, double source_offset, int is_arc,
+                     double ds, float offset, const double *xc, const double *yc, int nx, int ny,
+                     const uint8_t *mask, int ia_skip, int flags, void *stream) {
+    return back2_seam(image, sino, nb, na, sinb, cosb, is_arc ? SGB_ARC : SGB_FLAT, dsd, dso,
+                      source_offset, ds, offset, xc, yc, nx, ny, mask, ia_skip, flags, stream);
+}
+
+static int bdd_seam(bool forward, const float *in, int nPix, int nDet, int na, const double *angle,
+                    double DSD, double DS0, double pSize, double dSize, float *out, int flags,
+                    void *stream) {
+    SGB_REQUIRE(in && out && angle, "bdd: null argument");
+    SGB_REQUIRE(nPix > 0 && nDet > 0 && na > 0, "bdd: sizes must be positive");
+    cudaStream_t st = as_stream(stream);
+    DevBuf dang, scratch, din, dout;
+    SGB_TRY(upload_f64(angle, na, dang, st));
+    BddArgs G{nPix, nDet, na, dang.as<double>(), DSD, DS0, pSize, dSize};
+    SGB_TRY(scratch.reserve(forward ? bdd_project_scratch(G) : bdd_back_scratch(G)));
+    size_t nin = forward ? (size_t)nPix * nPix : (size_t)na * nDet;
+    size_t nout = forward ? (size_t)na * nDet : (size_t)nPix * nPix;
+    const void *in_dev;
+    SGB_TRY(stage_in(in, nin * sizeof(float), flags, din, &in_dev, st));
+    float *out_dev = out;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dout.reserve(nout * sizeof(float)));
+        out_dev = dout.as<float>();
+    }
+    if (forward) SGB_TRY(launch_bdd_project(G, static_cast<const float *>(in_dev), out_dev, scratch.p, st));
+    else SGB_TRY(launch_bdd_back(G, static_cast<const float *>(in_dev), out_dev, scratch.p, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(out, out_dev, nout * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int sgb_bdd_project(const float *phantom, int nPix, int nDet, int na, const double *angle,
+                    double DSD, double DS0, double pSize, double dSize, float *sino, int flags,
+                    void *stream) {
+    return bdd_seam(true, phantom, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, sino, flags, stream);
+}
+
+int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const double *angle,
+                        double DSD, double DS0, double pSize, double dSize, float *image, int flags,
+                        void *stream) {
+    return bdd_seam(false, sino, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, image, flags, stream);
+}
+
+int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nell, float *sino, int flags,
+                     void *stream) {
+    SGB_REQUIRE(rg && ell && sino && nell >= 0, "ellipse_sino: bad argument");
+    cudaStream_t st = as_stream(stream);
+    std::vector<double> s = det_axis(rg->nb, rg->d, rg->offset);
+    std::vector<double> b = view_angles(rg->na, rg->orbit, rg->orbit_start);
+    DevBuf ds_, db, de, dout;
+    SGB_TRY(upload_f64(s.data(), s.size(), ds_, st));
+    SGB_TRY(upload_f64(b.data(), b.size(), db, st));
+    SGB_TRY(upload_f64(ell, (size_t)6 * std::max(nell, 1), de, st));
+    size_t n = (size_t)rg->nb * rg->na;
+    float *out_dev = sino;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dout.reserve(n * sizeof(float)));
+        out_dev = dout.as<float>();
+    }
+    SGB_TRY(launch_ellipse_sino(rg->kind, rg->nb, rg->na, ds_.as<double>(), db.as<double>(),
+                                rg->dsd - rg->dod, rg->dsd, de.as<double>(), nell, out_dev, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(sino, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int sgb_ellipsoid_proj(const sgb_ct_geom *rg, const double *ell, int nell, float *proj, int flags,
+                       void *stream) {
+    SGB_REQUIRE(rg && ell && proj && nell >= 0, "ellipsoid_proj: bad argument");
+    cudaStream_t st = as_stream(stream);
+    std::vector<double> s = det_axis(rg->ns, rg->ds, rg->offset_s);
+    std::vector<double> t = det_axis(rg->nt, rg->dt, rg->offset_t);
+    std::vector<double> b = view_angles(rg->na, rg->orbit, rg->orbit_start);
+    DevBuf ds_, dt_, db, de, dout;
+    SGB_TRY(upload_f64(s.data(), s.size(), ds_, st));
+    SGB_TRY(upload_f64(t.data(), t.size(), dt_, st));
+    SGB_TRY(upload_f64(b.data(), b.size(), db, st));
+    SGB_TRY(upload_f64(ell, (size_t)10 * std::max(nell, 1), de, st));
+    size_t n = (size_t)rg->ns * rg->nt * rg->na;
+    float *out_dev = proj;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dout.reserve(n * sizeof(float)));
+        out_dev = dout.as<float>();
+    }
+    SGB_TRY(launch_ellipsoid_proj(rg->kind == SGB_ARC, rg->ns, rg->nt, rg->na, ds_.as<double>(),
+                                  dt_.as<double>(), db.as<double>(), rg->dsd - rg->dod, rg->dsd,
+                                  de.as<double>(), nell, out_dev, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(proj, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+}  // extern "C"

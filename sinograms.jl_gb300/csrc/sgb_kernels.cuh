@@ -1,0 +1,82 @@
+// sgb_kernels.cuh -- launch interfaces of the CUDA kernels (internal).
+#pragma once
+#include <vector>
+
+#include "sgb_common.cuh"
+
+namespace sgb {
+
+// ------------------------------------------------------------ row filter
+struct FilterArgs {
+    const float *in;     // (ns, nrows)
+    int ns;              // samples per row (nb)
+    int nout;            // output row length (ns + extra)
+    long long nrows;     // nt * na * nslices
+    int nt, na;          // row r -> t = r % nt, a = (r / nt) % na
+    const float *wA;     // A[j*sAj + a*sAa] or null
+    long long sAj, sAa;
+    const float *wB;     // B[j*sBj + t*sBt] or null
+    long long sBj, sBt;
+    float scale;         // scalar weight (dbeta)
+    const float *gext;   // (2ns-1) Toeplitz kernel
+};
+int launch_filter_rows(const FilterArgs &A, void *out, int out_bf16, cudaStream_t st);
+void build_gext(const std::vector<double> &g, int ns, std::vector<float> &gext);
+size_t filter_smem_bytes(int ns);
+
+// ---------------------------------------------------- view geometry table
+// per used view v (view index a = v * ia_skip): (sin, cos) in FP32 from FP64 angles.
+int launch_view_trig(const double *betas_dev, int na, int ia_skip, float2 *trig, cudaStream_t st);
+
+// -------------------------------------------------- FDK back-projection
+struct FdkArgs {
+    const void *proj;      // (ns, nt, na) float or bf16 filtered projections
+    float *image;          // (nx, ny, nz)
+    const uint8_t *mask;   // (nx, ny, nz) or null
+    const float2 *trig;    // nv used views
+    const float *xds, *yds, *zds;  // pixel centres / ds
+    int ns, nt, na, nx, ny, nz, nv, ia_skip;
+    float ws, wt;          // (ns+1)/2 + offset_s, (nt+1)/2 + offset_t (1-based)
+    float dsd_ds, dso_ds, inv_dtds;
+    int is_arc;
+    int bf16;
+};
+int launch_fdk_back(const FdkArgs &A, cudaStream_t st);
+
+// ---------------------------------------------- 2D pixel-driven back-projection
+struct Back2Args {
+    const float *sino;     // (nb, na, nslices)
+    float *image;          // (nx, ny, nslices)
+    const uint8_t *mask;   // (nx, ny) or null
+    const float2 *trig;    // nv used views: (sin, cos)
+    const float *xds, *yds;
+    int nb, na, nx, ny, nv, ia_skip, nslices;
+    float wb;
+    int mode;              // SGB_PAR, SGB_ARC, SGB_FLAT
+    float dsd_ds, dso_ds, so_ds;
+};
+int launch_back2(const Back2Args &A, cudaStream_t st);
+
+// ------------------------------------------------------- distance-driven pair
+struct BddArgs {
+    int nPix, nDet, na;
+    const double *angle;   // device, na
+    double DSD, DS0, pSize, dSize;
+};
+// scratch sizes are returned by the *_scratch functions (bytes).
+size_t bdd_project_scratch(const BddArgs &G);
+int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
+                       cudaStream_t st);
+size_t bdd_back_scratch(const BddArgs &G);
+int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scratch,
+                    cudaStream_t st);
+
+// -------------------------------------------------------- analytic phantoms
+int launch_ellipse_sino(int kind, int nb, int na, const double *s_dev, const double *beta_dev,
+                        double dso, double dsd, const double *ell_dev, int nell, float *sino,
+                        cudaStream_t st);
+int launch_ellipsoid_proj(int is_arc, int ns, int nt, int na, const double *s_dev,
+                          const double *t_dev, const double *beta_dev, double dso, double dsd,
+                          const double *ell_dev, int nell, float *proj, cudaStream_t st);
+
+}  // namespace sgb

@@ -1,0 +1,17 @@
+"""sinograms -- host-side mirror of the Sinograms.jl API over libsinogb300.so.
+
+Names, argument meaning and error behaviour follow the reference package
+(JuliaImageRecon/Sinograms.jl v0.5.1); every computation runs in the CUDA library
+(include/sinogb300.h).  See geom.py for the array-order convention.
+"""
+from ._lib import SinogramsError, launch_count
+from .bdd import BddGeo, backproject_bdd, project_bdd
+from .filters import (SinogramsArgumentError, Window, _angle_weights, fbp_filter, fbp_ramp, fbp_sino_filter,
+                      fbp_sino_weight, fbp_window, fdk_view_weight, fbp_view_weight, fdk_weight_cyl, parker_weight,
+                      ramp_arc, ramp_flat)
+from .geom import (CtFanArc, CtFanFlat, ImageGeom, SinoFanArc, SinoFanFlat, SinoPar, _ar, _dso, _gamma, _gamma_max,
+                   _orbit_short, _rfov, _s, _t, angles, axes, dims, downsample)
+from .phantoms import ellipse_sino, ellipsoid_proj, random_ellipses, random_ellipsoids
+from .recon import FBPNormalPlan, FDKplan, cbct_back, fbp, fbp_back, fdk, plan_fbp
+
+__all__ = [n for n in dir() if not n.startswith("__")]

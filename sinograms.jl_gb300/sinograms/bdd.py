@@ -1,0 +1,64 @@
+"""Branchless distance-driven projector pair, src/sys2/bdd_2d.jl, on the GPU.
+
+``geo`` is the reference's named tuple: DSD, DS0, pSize, dSize, nPix, nDet, angle.
+Layouts follow the reference: the phantom is Julia (nPix, nPix) with row = y (row 1 at
+the top) and col = x, i.e. numpy ``phantom_np[col, row]``; the sinogram is Julia
+(na, nDet), i.e. numpy ``(nDet, na)``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._arrays import Arr, empty, f64, flags_for, ptr, stream_for
+from .filters import SinogramsArgumentError
+from .geom import _ar, _dso
+
+
+@dataclass
+class BddGeo:
+    DSD: float
+    DS0: float
+    pSize: float
+    dSize: float
+    nPix: int
+    nDet: int
+    angle: np.ndarray
+
+    @classmethod
+    def from_geoms(cls, rg, ig):
+        """geo tuple as built in test/sys2/bdd_2d.jl:45-46 from SinoFanFlat + ImageGeom."""
+        return cls(rg.dsd, _dso(rg), ig.deltas[0], rg.d, ig.dims[0], rg.nb, _ar(rg))
+
+
+def _g(geo, k):
+    return geo[k] if isinstance(geo, dict) else getattr(geo, k)
+
+
+def _run(fn, x, geo, out_shape):
+    a = Arr(x)
+    ang = f64(_g(geo, "angle"))
+    out = empty(out_shape, a)
+    st = getattr(_lib.lib(), fn)(a.ptr, int(_g(geo, "nPix")), int(_g(geo, "nDet")), len(ang), ptr(ang),
+                                 float(_g(geo, "DSD")), float(_g(geo, "DS0")), float(_g(geo, "pSize")),
+                                 float(_g(geo, "dSize")), ptr(out), flags_for(a.device), stream_for(a.device))
+    if st == _lib.SGB_ERR_ARG:
+        raise SinogramsArgumentError(_lib.last_error())
+    _lib.check(st, fn)
+    return out
+
+
+def project_bdd(phantom, geo):
+    """sinogram = project_bdd(phantom, geo), bdd_2d.jl:17-110 (numpy (nDet, na) out)."""
+    n = int(_g(geo, "nPix"))
+    if tuple(Arr(phantom).shape) != (n, n):
+        raise SinogramsArgumentError("phantom must be (nPix, nPix)")
+    return _run("sgb_bdd_project", phantom, geo, (int(_g(geo, "nDet")), len(_g(geo, "angle"))))
+
+
+def backproject_bdd(sinogram, geo):
+    """image = backproject_bdd(sinogram, geo), bdd_2d.jl:119-220 (numpy (nPix, nPix))."""
+    n = int(_g(geo, "nPix"))
+    return _run("sgb_bdd_backproject", sinogram, geo, (n, n))

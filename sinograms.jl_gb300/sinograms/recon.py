@@ -1,0 +1,203 @@
+"""Reconstruction: plan_fbp / fbp / fdk / cbct_back / fbp_back on the GPU library.
+
+Mirrors src/fbp2/plan2.jl, fbp.jl, fbp-par.jl, back-par.jl, back-fan.jl and
+src/fbp3/plan3.jl, fdk.jl, cbct-back.jl.  All arithmetic happens in libsinogb300.so.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._arrays import Arr, empty, f64, flags_for, ptr, stream_for
+from .filters import SinogramsArgumentError, Window, fbp_filter, fdk_view_weight, fbp_view_weight
+from .geom import CtFan, ImageGeom, SinoPar, _ar, _dso, _rfov, c_struct, dims, is_ct
+
+
+def _status(st: int, what: str):
+    if st in (_lib.SGB_ERR_ARG, _lib.SGB_ERR_GEOM):
+        raise SinogramsArgumentError(f"{what}: {_lib.last_error()}")
+    _lib.check(st, what)
+
+
+class _Plan:
+    """Owner of a library plan handle (sgb_plan)."""
+
+    def __init__(self, rg, ig: ImageGeom, window: Window, npad, decon1, filter, storage):
+        self.rg, self.ig = rg, ig
+        self.window = window
+        self.storage = storage
+        opts = _lib.FilterOptsC()
+        self._keep = []
+        if isinstance(window.shape, str):
+            opts.window_shape = _lib.SGB_WIN[window.shape]
+        else:
+            v = f64(window.shape)
+            self._keep.append(v)
+            opts.window_shape = _lib.SGB_WIN["vect"]
+            opts.window_vect = v.ctypes.data
+        opts.cutoff = float(window.cutoff)
+        opts.npad = int(npad or 0)
+        opts.decon1 = int(decon1)
+        if filter is not None:
+            f = f64(filter)
+            self._keep.append(f)
+            opts.filter = f.ctypes.data
+            opts.npad = len(f)
+        opts.storage = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16}[storage]
+        self._h = ctypes.c_void_p()
+        g, cig = c_struct(rg), ig.c_struct()
+        fn = "sgb_plan_fbp_ct" if is_ct(rg) else "sgb_plan_fbp_sino"
+        _status(getattr(_lib.lib(), fn)(ctypes.byref(g), ctypes.byref(cig), ctypes.byref(opts),
+                                        ctypes.byref(self._h)), "plan_fbp")
+        n = ctypes.c_int()
+        _status(_lib.lib().sgb_plan_filter(self._h, None, ctypes.byref(n)), "plan_filter")
+        self.filter = np.zeros(n.value)
+        _status(_lib.lib().sgb_plan_filter(self._h, ptr(self.filter), ctypes.byref(n)), "plan_filter")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib._lib is not None:
+            _lib.lib().sgb_plan_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_timing(self, enable: bool = True):
+        """Record CUDA events around the filter and back-projection stages."""
+        _status(_lib.lib().sgb_plan_set_timing(self._h, int(enable)), "plan_set_timing")
+
+    def last_timing(self):
+        """(filter_ms, back_ms) of the last fdk/fbp call (needs set_timing)."""
+        ms = np.zeros(2)
+        _status(_lib.lib().sgb_plan_last_timing(self._h, ptr(ms), 2), "plan_last_timing")
+        return float(ms[0]), float(ms[1])
+
+
+class FBPNormalPlan(_Plan):
+    """FBPNormalPlan (plan2.jl:41-52): rg, ig, filter (Hk), view_weight."""
+
+    @property
+    def view_weight(self):
+        return fbp_view_weight(self.rg)
+
+
+class FDKplan(_Plan):
+    """FDKplan (plan3.jl:13-23): rg, ig, filter (Hk), view_weight."""
+
+    @property
+    def view_weight(self):
+        return fdk_view_weight(self.rg)
+
+
+def plan_fbp(rg, ig: ImageGeom, window: Window = Window(), npad: int | None = None, decon1: bool = True,
+             filter=None, storage: str = "f32"):
+    """plan_fbp(rg, ig; window, npad, decon1, filter), plan2.jl:106-138 / plan3.jl:60-72.
+
+    ``storage`` ("f32" or "bf16") selects how FDK keeps the filtered projections on the
+    GPU (an addition of this implementation; 2D plans always use "f32")."""
+    if is_ct(rg):
+        return FDKplan(rg, ig, window, npad, decon1, filter, storage)
+    if storage != "f32":
+        raise SinogramsArgumentError("2D plans keep filtered sinograms in f32")
+    return FBPNormalPlan(rg, ig, window, npad, decon1, filter, storage)
+
+
+def fdk(plan: FDKplan, proj, out=None, sync: bool = True):
+    """image = fdk(plan, proj), fdk.jl:65-81.  proj in numpy order (na, nt, ns) ->
+    image (nz, ny, nx).  CUDA tensors stay on the device."""
+    rg = plan.rg
+    a = Arr(proj)
+    if tuple(reversed(a.shape)) != dims(rg):
+        raise SinogramsArgumentError(f"size mismatch {tuple(reversed(a.shape))} {dims(rg)}")  # fdk.jl:68-69
+    img = out if out is not None else empty(tuple(reversed(plan.ig.dims)), a)
+    _status(_lib.lib().sgb_fdk(plan.handle, a.ptr, ptr(img), flags_for(a.device, sync), stream_for(a.device)), "fdk")
+    return img
+
+
+def _fbp_plan(plan: FBPNormalPlan, sino, out=None, sync=True):
+    rg = plan.rg
+    a = Arr(sino)
+    shp = tuple(reversed(a.shape))  # Julia order (nb, na, ...)
+    if shp[:2] != dims(rg):
+        raise SinogramsArgumentError("bad sino size")  # fbp.jl:80
+    nsl = int(np.prod(shp[2:])) if len(shp) > 2 else 1
+    oshape = tuple(reversed(plan.ig.dims)) if len(shp) == 2 else tuple(a.shape[:-2]) + tuple(reversed(plan.ig.dims))
+    img = out if out is not None else empty(oshape, a)
+    _status(_lib.lib().sgb_fbp(plan.handle, a.ptr, ptr(img), nsl, flags_for(a.device, sync), stream_for(a.device)),
+            "fbp")
+    return img
+
+
+def fbp(plan_or_sino, sino=None, *, out=None, sync=True, **kw):
+    """fbp(plan, sino) (fbp.jl:24-68; stacks too) or the convenience fbp(sino; dr, ...)
+    (fbp-par.jl:23-36, 63-89)."""
+    if isinstance(plan_or_sino, _Plan):
+        return _fbp_plan(plan_or_sino, sino, out, sync)
+    return _fbp_simple(plan_or_sino, **kw)
+
+
+def _fbp_simple(sino, nx=None, ny=None, dr=1.0, dx=None, dy=None, orbit=180.0, orbit_start=0.0,
+                offset_x=0.0, offset_y=0.0, rmax=0.0, **plan_kw):
+    """fbp(sino; dr, ...) -> fbp!, fbp-par.jl:23-89: SinoPar + ImageGeom with a disk mask."""
+    a = Arr(sino)
+    na, nb = a.shape
+    nx = nx or nb
+    ny = ny or nx
+    dx = dr if dx is None else dx
+    dy = dx if dy is None else dy
+    rg = SinoPar(nb=nb, na=na, d=dr, orbit=orbit, orbit_start=orbit_start)
+    ig = ImageGeom((nx, ny), (dx, dy), (offset_x, offset_y))
+    ig = ig.with_mask(ig.circle(_rfov(rg) if rmax == 0 else rmax))
+    return _fbp_plan(plan_fbp(rg, ig, **plan_kw), sino)
+
+
+def cbct_back(proj, rg, ig: ImageGeom, ia_skip: int = 1, sync: bool = True):
+    """cbct_back(proj, rg, ig; ia_skip), cbct-back.jl:25-45 (pure back-projection)."""
+    if not isinstance(rg, CtFan):
+        raise SinogramsArgumentError("cbct_back needs a CtFan geometry")
+    a = Arr(proj)
+    na, nt, ns = a.shape
+    xc, yc, zc = (f64(v) for v in ig.axes())
+    betas = f64(_ar(rg))
+    mask = None
+    if ig.mask is not None:
+        mask = Arr(ig.mask if not a.device else __import__("torch").as_tensor(ig.mask, device=a.obj.device),
+                   dtype=np.uint8)
+    img = empty(tuple(reversed(ig.dims)), a)
+    _status(_lib.lib().sgb_cbct_back(ptr(img), a.ptr, ns, nt, na, ptr(betas), rg.dsd, _dso(rg), rg.ds, rg.dt,
+                                     rg.offset_s, rg.offset_t, int(rg.kind == "arc"), ptr(xc), ptr(yc), ptr(zc),
+                                     ig.dims[0], ig.dims[1], ig.dims[2], None if mask is None else mask.ptr,
+                                     ia_skip, flags_for(a.device, sync), stream_for(a.device)), "cbct_back")
+    return img
+
+
+def fbp_back(rg, ig: ImageGeom, sino, ia_skip: int = 1):
+    """fbp_back(rg, ig, sino; ia_skip), back-par.jl:184-203 / back-fan.jl:11-32."""
+    a = Arr(sino)
+    if tuple(reversed(a.shape)) != dims(rg):
+        raise SinogramsArgumentError("sino size")
+    na, nb = a.shape
+    xc, yc = (f64(v) for v in ig.axes())
+    ar = _ar(rg)[::ia_skip]
+    sn, cs = f64(np.sin(ar)), f64(np.cos(ar))
+    mask = None
+    if ig.mask is not None:
+        mask = Arr(ig.mask if not a.device else __import__("torch").as_tensor(ig.mask, device=a.obj.device),
+                   dtype=np.uint8)
+    img = empty(tuple(reversed(ig.dims)), a)
+    mptr = None if mask is None else mask.ptr
+    if rg.kind == "par":
+        st = _lib.lib().sgb_fbp_back_par(ptr(img), a.ptr, nb, na, ptr(sn), ptr(cs), rg.d, rg.offset, ptr(xc),
+                                         ptr(yc), ig.dims[0], ig.dims[1], mptr, ia_skip, flags_for(a.device),
+                                         stream_for(a.device))
+    else:
+        st = _lib.lib().sgb_fbp_back_fan(ptr(img), a.ptr, nb, na, ptr(sn), ptr(cs), rg.dsd, _dso(rg),
+                                         rg.source_offset, int(rg.kind == "arc"), rg.d, rg.offset, ptr(xc),
+                                         ptr(yc), ig.dims[0], ig.dims[1], mptr, ia_skip, flags_for(a.device),
+                                         stream_for(a.device))
+    _status(st, "fbp_back")
+    return img

@@ -1,0 +1,73 @@
+"""Geometries of the golden fixtures and parity cases, as plain parameter dicts.
+
+Shared by tests/golden/make_fixtures.py (oracle side) and the tests (library side), so
+both see identical inputs.  ``to_geom`` builds the library's geometry objects.
+"""
+import math
+
+import numpy as np
+
+ELL3 = np.array([[2.0, 3.0, 1.0, 6.0, 5.0, 4.0, 0.3, 0.4, 0.1, 1.0],
+                 [-3.0, -1.0, -2.0, 3.0, 2.0, 4.0, 1.0, 0.2, 0.5, -0.4],
+                 [0.0, 0.0, 2.0, 1.5, 1.5, 1.5, 0.0, 0.0, 0.0, 0.8]])
+ELL2 = np.array([[1.0, 0.5, 2.0, 1.5, 0.3, 1.0], [-1.0, -1.0, 1.0, 0.7, 1.2, -0.5]])
+
+
+def gamma_max(g):
+    n = g["ns"] if "ns" in g else g["nb"]
+    d = g["ds"] if "ns" in g else g["d"]
+    off = float(np.float32(g.get("offset_s", g.get("offset", 0.0))))
+    s = d * (np.arange(n) - ((n - 1) / 2 + off))
+    gam = s / g["dsd"] if g["kind"] == "arc" else np.arctan(s / g["dsd"])
+    return float(np.max(np.abs(gam)))
+
+
+def short(g, na):
+    """The `:short` constructor (type2.jl:281-288, type3.jl:333-341)."""
+    os_ = 180 + 2 * math.degrees(gamma_max(dict(g, orbit=360.0)))
+    return dict(g, na=math.ceil(na * os_ / 360), orbit=os_)
+
+
+def ct(kind, **kw):
+    g = dict(kind=kind, ns=32, nt=24, ds=1.0, dt=1.2, offset_s=0.0, offset_t=0.0, na=24, orbit=360.0,
+             orbit_start=0.0, source_offset=0.0, dsd=128.0, dod=32.0)
+    g.update(kw)
+    return g
+
+
+FDK_FLAT = dict(rg=ct("flat", offset_s=0.25, offset_t=-0.5),
+                ig=dict(dims=(16, 14, 12), deltas=(1.0, 1.1, 0.9), offsets=(0.5, -0.25, 0.3)), window="none")
+FDK_ARC_SHORT = dict(rg=short(ct("arc"), 24), ig=dict(dims=(16, 14, 12), deltas=(1.0, 1.0, 1.0)), mask_r=6.0,
+                     window="hann", cutoff=0.8)
+PAR = dict(rg=dict(kind="par", nb=40, d=0.5, offset=0.25, na=36, orbit=180.0, orbit_start=0.0),
+           ig=dict(dims=(24, 20), deltas=(0.5, 0.5)), window="hann")
+_ARC = dict(kind="arc", nb=40, d=0.5, offset=0.0, na=48, orbit=360.0, orbit_start=0.0, source_offset=0.0,
+            dsd=80.0, dod=20.0)
+ARC_SHORT = dict(rg=short(_ARC, 48), ig=PAR["ig"], window="none")
+FLAT = dict(rg=dict(_ARC, kind="flat"), ig=PAR["ig"], window="hamming")
+BDD = dict(DSD=300.0, DS0=180.0, pSize=2.0, dSize=2.3, nPix=32, nDet=40, angle=np.arange(24) * (2 * math.pi / 24))
+FILTER_WRAP = dict(nb=24, npad=32, extra=3, rows=5)
+
+
+def cyl_mask(ig, r):
+    dims, deltas = ig["dims"], ig["deltas"]
+    ax = [d * (np.arange(n) - (n - 1) / 2) for n, d in zip(dims, deltas)]
+    m2 = (ax[0][None, :] ** 2 + ax[1][:, None] ** 2) <= r * r
+    return np.broadcast_to(m2[None], (dims[2],) + m2.shape).copy() if len(dims) == 3 else m2
+
+
+def to_geom(g):
+    """Library geometry object for a parameter dict."""
+    import sinograms as S
+    g = dict(g)
+    kind = g.pop("kind")
+    if "ns" in g:
+        return (S.CtFanArc if kind == "arc" else S.CtFanFlat)(**g)
+    if kind == "par":
+        return S.SinoPar(**g)
+    return (S.SinoFanArc if kind == "arc" else S.SinoFanFlat)(**g)
+
+
+def to_image(ig, mask=None):
+    import sinograms as S
+    return S.ImageGeom(ig["dims"], ig["deltas"], ig.get("offsets"), mask)

@@ -1,0 +1,207 @@
+"""GPU parity: every CUDA entry point against the FP64 oracle (committed fixtures and live
+oracle runs on the same seeded inputs), plus the reference's conservation tests run on
+the GPU path.
+
+Tolerances (FP32 arithmetic against FP64): relative RMSE <= 1e-5 and max abs error
+<= 1e-4 * max|ref| for the FP32 forms; <= 1e-4 relative RMSE for the BF16 storage form
+(the benchmark spec's bound)."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import cases as C
+import oracle as O
+import sinograms as S
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+RTOL_RMSE = 1e-5
+MAX_REL = 1e-4
+
+
+def fix(name):
+    return np.load(os.path.join(HERE, "golden", f"{name}.npz"))
+
+
+def close(x, ref, rmse=RTOL_RMSE, maxrel=MAX_REL):
+    x = np.asarray(x, np.float64)
+    ref = np.asarray(ref, np.float64)
+    assert x.shape == ref.shape, (x.shape, ref.shape)
+    e = O.rel_rmse(x, ref)
+    m = np.abs(x - ref).max() / np.abs(ref).max()
+    assert e <= rmse and m <= maxrel, f"rel_rmse={e:.3g} max_rel={m:.3g}"
+    return e
+
+
+def test_fdk_flat_fixture(cuda):
+    f, c = fix("fdk_flat"), C.FDK_FLAT
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), window=S.Window(c["window"]))
+    close(S.fdk(plan, f["proj"]), f["ref"])
+
+
+def test_fdk_arc_short_fixture_mask_window(cuda):
+    f, c = fix("fdk_arc_short"), C.FDK_ARC_SHORT
+    mask = C.cyl_mask(c["ig"], c["mask_r"])
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"], mask), window=S.Window(c["window"], c["cutoff"]))
+    out = S.fdk(plan, f["proj"])
+    close(out, f["ref"])
+    assert np.all(out[~mask] == 0)
+
+
+@pytest.mark.parametrize("name,case", [("fbp_par", C.PAR), ("fbp_arc_short", C.ARC_SHORT), ("fbp_flat", C.FLAT)])
+def test_fbp_fixtures(cuda, name, case):
+    f = fix(name)
+    plan = S.plan_fbp(C.to_geom(case["rg"]), C.to_image(case["ig"]), window=S.Window(case["window"]))
+    close(S.fbp(plan, f["sino"]), f["ref"])
+
+
+def test_sino_filter_wrap_fixture(cuda):
+    f = fix("sino_filter_wrap")
+    close(S.fbp_sino_filter(f["x"], f["Hk"], extra=C.FILTER_WRAP["extra"]), f["ref"], maxrel=2e-4)
+
+
+@pytest.mark.parametrize("nb,npad", [(64, 128), (100, 128), (512, 1024), (888, 1024), (37, 64)])
+def test_sino_filter_random(cuda, nb, npad):
+    rng = np.random.default_rng(nb)
+    x = rng.standard_normal((9, 3, nb)).astype(np.float32)
+    Hk = O.fbp_filter(dict(kind="flat", nb=nb, d=1.0), npad=npad, shape="hann")
+    close(S.fbp_sino_filter(x, Hk), O.sino_filter(x, Hk), maxrel=2e-4)
+
+
+def test_bdd_fixtures(cuda):
+    f, g = fix("bdd"), C.BDD
+    geo = S.BddGeo(g["DSD"], g["DS0"], g["pSize"], g["dSize"], g["nPix"], g["nDet"], g["angle"])
+    close(S.project_bdd(f["phantom"], geo), f["ref_proj"])
+    close(S.backproject_bdd(f["sino"], geo), f["ref_back"])
+
+
+@pytest.mark.parametrize("kind", ["arc", "flat"])
+@pytest.mark.parametrize("ia_skip", [1, 3])
+def test_cbct_back_seam(cuda, kind, ia_skip):
+    rg = C.ct(kind, ns=40, nt=30, na=25, offset_s=0.25)
+    ig = dict(dims=(20, 18, 14), deltas=(1.0, 1.0, 1.3), offsets=(0.0, 0.5, -0.5))
+    rng = np.random.default_rng(3)
+    proj = rng.standard_normal((25, 30, 40)).astype(np.float32)
+    mask = rng.random((14, 18, 20)) > 0.2
+    ref = O.cbct_back(proj, rg, dict(ig, mask=mask), ia_skip=ia_skip)
+    out = S.cbct_back(proj, C.to_geom(rg), C.to_image(ig, mask), ia_skip=ia_skip)
+    close(out, ref)
+
+
+@pytest.mark.parametrize("case", [C.PAR, C.ARC_SHORT, C.FLAT], ids=["par", "arc", "flat"])
+def test_fbp_back_seam_ia_skip(cuda, case):
+    rng = np.random.default_rng(5)
+    rg = case["rg"]
+    s = rng.standard_normal((rg["na"], rg["nb"])).astype(np.float32)
+    ax = O.image_axes(case["ig"])
+    mask = (ax[0][None, :] ** 2 + ax[1][:, None] ** 2) <= 4.0 ** 2
+    for skip in (1, 2):
+        ref = O.fbp_back(rg, dict(case["ig"], mask=mask), s, ia_skip=skip)
+        out = S.fbp_back(C.to_geom(rg), C.to_image(case["ig"], mask), s, ia_skip=skip)
+        close(out, ref)
+
+
+def test_device_pointer_path_equals_host(cuda):
+    import torch
+    f, c = fix("fdk_flat"), C.FDK_FLAT
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]))
+    host = S.fdk(plan, f["proj"])
+    dev = S.fdk(plan, torch.as_tensor(f["proj"], device="cuda"))
+    assert isinstance(dev, torch.Tensor) and dev.is_cuda
+    np.testing.assert_array_equal(dev.cpu().numpy(), host)
+
+
+def test_fbp_stack_equals_slices(cuda):
+    """fbp(plan, sino3) loops the 2D path over slices (fbp.jl:46-68); linearity x5
+    as in test/fbp2/fbp-par.jl:79-83."""
+    f, c = fix("fbp_par"), C.PAR
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), window=S.Window(c["window"]))
+    one = S.fbp(plan, f["sino"])
+    stack = S.fbp(plan, np.stack([f["sino"], 5 * f["sino"]]))
+    np.testing.assert_allclose(stack[0], one, rtol=0, atol=0)
+    np.testing.assert_allclose(stack[1], 5 * one, rtol=1e-5, atol=1e-6 * np.abs(one).max())
+
+
+def test_phantom_projectors(cuda):
+    g = C.ARC_SHORT["rg"]
+    close(S.ellipse_sino(C.to_geom(g), C.ELL2), O.ellipse_sino(g, C.ELL2), rmse=1e-7, maxrel=1e-6)
+    rg = C.FDK_FLAT["rg"]
+    close(S.ellipsoid_proj(C.to_geom(rg), C.ELL3), O.ellipsoid_proj(rg, C.ELL3), rmse=1e-5, maxrel=1e-4)
+
+
+# ------------------------------------------------ reference conservation tests on the GPU
+
+def _disk_err(rec, dx):
+    return abs(float(np.sum(rec, dtype=np.float64)) * dx * dx - math.pi * 4) / (math.pi * 4)
+
+
+def test_gpu_fbp_par_conservation(cuda):
+    nr, dr, na = 64, 10 / 64, 128  # test/fbp2/fbp-par.jl:12-33
+    rg = S.SinoPar(nb=nr, d=dr, na=na)
+    s = S.ellipse_sino(rg, [[2.0, 1.0, 2.0, 2.0, 0.0, 1.0]])
+    assert _disk_err(S.fbp(s, dr=dr), dr) < 2e-4
+    rg = S.SinoPar(d=0.1)  # :35-49
+    ig = S.ImageGeom((128, 128), (0.1, 0.1))
+    ig = ig.with_mask(ig.circle(S._rfov(rg)))
+    s = S.ellipse_sino(rg, [[2.0, 1.0, 2.0, 2.0, 0.0, 1.0]])
+    rec = S.fbp(S.plan_fbp(rg, ig), np.stack([s, 5 * s]))
+    assert _disk_err(rec[0], 0.1) < 5e-4 and _disk_err(rec[1] / 5, 0.1) < 5e-4
+
+
+@pytest.mark.parametrize("cls", [S.SinoFanArc, S.SinoFanFlat])
+@pytest.mark.parametrize("short", [False, True])
+def test_gpu_fbp_fan_conservation(cuda, cls, short):
+    rg = cls.short(d=0.1) if short else cls(d=0.1)  # test/fbp2/fbp-fan.jl:13-40
+    ig = S.ImageGeom((128, 128), (0.1, 0.1))
+    ig = ig.with_mask(ig.circle(S._rfov(rg)))
+    s = S.ellipse_sino(rg, [[2.0, 1.0, 2.0, 2.0, 0.0, 1.0]])
+    assert _disk_err(S.fbp(S.plan_fbp(rg, ig), s), 0.1) < 3e-3
+
+
+@pytest.mark.parametrize("cls", [S.CtFanArc, S.CtFanFlat])
+@pytest.mark.parametrize("short", [False, True])
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_gpu_fdk_conservation(cuda, cls, short, storage):
+    kw = dict(ns=64, nt=40, ds=1.0, dt=1.2)  # test/fbp3/fdk.jl:14-33
+    rg = cls.short(na=59, **kw) if short else cls(na=32, **kw)
+    ig = S.ImageGeom((30, 28, 26), (1.0, 1.0, 1.0))
+    proj = S.ellipsoid_proj(rg, [[2.0, 3.0, 4.0, 8.0, 7.0, 6.0, 0.0, 0.0, 0.0, 1.0]])
+    rec = S.fdk(S.plan_fbp(rg, ig, storage=storage), proj)
+    vt = 4 / 3 * math.pi * 8 * 7 * 6
+    assert abs(float(rec.sum(dtype=np.float64)) - vt) / vt < (2e-2 if short else 3e-3)
+
+
+def test_gpu_bdd_adjoint_and_shapes(cuda):
+    rg = S.downsample(S.SinoFanFlat(nb=910, d=1.0239, na=360, dsd=949.0, dod=408.0), 4)  # test/sys2/bdd_2d.jl
+    ig = S.ImageGeom((128, 128), (4.0, 4.0))
+    geo = S.BddGeo.from_geoms(rg, ig)
+    rng = np.random.default_rng(0)
+    x = rng.random((128, 128)).astype(np.float32)
+    y = rng.random((rg.nb, rg.na)).astype(np.float32)
+    Ax, Aty = S.project_bdd(x, geo), S.backproject_bdd(y, geo)
+    assert Ax.shape == (geo.nDet, len(geo.angle)) and Aty.shape == (128, 128)
+    lhs, rhs = float(np.dot(Ax.ravel().astype(np.float64), y.ravel())), float(np.dot(x.ravel(), Aty.ravel()))
+    assert lhs == pytest.approx(rhs, rel=2e-2)
+    ogeo = O.bdd_geo(geo.DSD, geo.DS0, geo.pSize, geo.dSize, geo.nPix, geo.nDet, geo.angle)
+    close(Ax, O.project_bdd(x, ogeo))
+    close(Aty, O.backproject_bdd(y, ogeo))
+
+
+# -------------------------------------------------------------- BF16 storage form
+
+def test_fdk_bf16_form_within_north_star_bound(cuda):
+    """BF16 filtered projections: <= 1e-4 relative RMSE against the FP64 oracle on a
+    seeded random-ellipsoid phantom (the benchmark's phantom family, reduced size)."""
+    rg = S.CtFanFlat(ns=128, nt=96, ds=1.0, dt=1.0, dsd=1000.0, dod=400.0, na=180)
+    ig = S.ImageGeom((96, 96, 64), (1.0, 1.0, 1.0))
+    ell = S.random_ellipsoids(30, 3, 25.0, 12.0, axes=(3.0, 20.0))
+    proj = S.ellipsoid_proj(rg, ell)
+    orc = dict(kind="flat", ns=128, nt=96, ds=1.0, dt=1.0, offset_s=0.0, offset_t=0.0, na=180, orbit=360.0,
+               orbit_start=0.0, source_offset=0.0, dsd=1000.0, dod=400.0)
+    ref = O.fdk(orc, dict(dims=(96, 96, 64), deltas=(1.0, 1.0, 1.0)), proj)
+    e32 = O.rel_rmse(S.fdk(S.plan_fbp(rg, ig), proj), ref)
+    e16 = O.rel_rmse(S.fdk(S.plan_fbp(rg, ig, storage="bf16"), proj), ref)
+    assert e32 < 1e-5
+    assert e16 < 1e-4, e16

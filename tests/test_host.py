@@ -1,0 +1,111 @@
+"""CPU tests of the library's host side: it loads, exports every symbol the public
+header declares, and its plan-time FP64 arithmetic and error behaviour match the oracle
+and the reference (no GPU needed: these entry points run on the host)."""
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+import cases as C
+import oracle as O
+import sinograms as S
+from sinograms import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+KA = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_known_answers.json")))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "sinogb300.h")).read()
+    return sorted(set(re.findall(r"^SGB_API\s+(?:int|long long)\s+(sgb_\w+)\s*\(", txt, flags=re.M)))
+
+
+def test_library_exports_every_header_symbol():
+    L = _lib.lib()
+    syms = header_symbols()
+    assert len(syms) >= 20
+    for s in syms:
+        assert hasattr(L, s), s
+    assert set(syms) <= set(_lib.exported_symbols())  # the ctypes table covers the header
+    assert L.sgb_version() >= 10000
+
+
+GEOMS = [
+    S.SinoPar(), S.SinoPar(orbit=270), S.SinoPar(nb=64, d=0.5, offset=0.25, orbit=360),
+    S.SinoFanArc(), S.SinoFanArc.short(), S.SinoFanFlat(nb=64, d=0.5, offset=0.25),
+    S.SinoFanFlat.short(nb=96, d=0.7, dsd=300.0, dod=100.0), S.SinoFanArc.ge1(orbit="short"),
+    S.CtFanArc(), S.CtFanArc.short(ns=64, nt=40, ds=1.0, dt=1.2, na=59),
+    S.CtFanFlat(ns=64, nt=40, ds=1.0, dt=1.2, na=32), S.CtFanFlat.short(ns=48, nt=16, offset_s=0.25, na=40),
+]
+
+
+@pytest.mark.parametrize("rg", GEOMS, ids=lambda g: f"{type(g).__name__}-{g.na}")
+def test_plan_time_tables_match_oracle(rg):
+    for win in (S.Window(), S.Window("hann", 0.8), S.Window("hamming"), S.Window("boxcar", 0.5)):
+        Hk = S.fbp_filter(rg, window=win)
+        Ho = O.fbp_filter(rg, shape=win.shape, cutoff=win.cutoff)
+        np.testing.assert_allclose(Hk, Ho, rtol=1e-12, atol=1e-13 * np.abs(Ho).max())
+    pw, po = S.parker_weight(rg), O.parker_weight(rg)
+    assert pw.shape == po.shape and np.array_equal(pw.astype(np.float64), po)
+    assert S._angle_weights(S._ar(rg)) == pytest.approx(O.angle_weight(rg), rel=1e-15)
+    if isinstance(rg, S.geom.CtFan):
+        np.testing.assert_allclose(S.fdk_weight_cyl(rg), O.fdk_weight_cyl(rg), rtol=1e-14)
+        np.testing.assert_allclose(S.fdk_view_weight(rg), O.fdk_weights(rg), rtol=1e-6)
+    elif rg.kind != "par":
+        np.testing.assert_allclose(S.fbp_sino_weight(rg), O.fbp_sino_weight(rg), rtol=1e-14)
+
+
+def test_ramp_and_window():
+    for N, ds, dsd in ((8, 2.0, 99.0), (6, 1.0, 50.0), (1024, 1.0239, 949.075)):
+        np.testing.assert_allclose(S.ramp_flat(N, ds)[0], O.ramp(dict(kind="flat", ds=ds, ns=2), N), rtol=1e-15)
+        np.testing.assert_allclose(S.ramp_arc(N, ds, dsd)[0], O.ramp(dict(kind="arc", ds=ds, ns=2, dsd=dsd), N),
+                                   rtol=1e-14)
+        assert list(S.ramp_flat(N, ds)[1]) == list(range(-(N // 2), N // 2))
+    w = S.fbp_window(S.Window("hamming"), 4)
+    assert np.array_equal(w.astype(np.float32), np.array(KA["window"]["hamming_N4"]["value"], np.float32))
+    assert S.fbp_window(S.Window(np.arange(1, 9)), 8)[0] == 5
+    for sh in ("none", "boxcar", "hamming", "hann"):
+        assert S.fbp_window(S.Window(sh, 0.7), 8)[0] == 1
+
+
+def test_errors_like_reference():
+    with pytest.raises(S.SinogramsArgumentError, match="N must be even"):
+        S.ramp_flat(7, 1.0)  # ramp.jl:234
+    with pytest.raises(S.SinogramsArgumentError, match="physically impossible"):
+        S.ramp_arc(4096, 1.0, 100.0)  # ramp.jl:217-219
+    with pytest.raises(S.SinogramsArgumentError, match="N mismatch"):
+        S.fbp_window(S.Window(np.ones(7)), 8)  # window.jl:310
+    with pytest.raises(S.SinogramsArgumentError, match="Parker"):
+        S.parker_weight(S.SinoPar(orbit=361))  # parker.jl:45
+    with pytest.raises(S.SinogramsArgumentError, match="Unequal"):
+        S._angle_weights([0.0, 0.1, 0.3])  # d-angle.jl:57
+
+
+def test_geometry_defaults_match_doctests():
+    d = KA["defaults"]
+    for cls, key in ((S.SinoPar, "SinoPar"), (S.SinoFanArc, "SinoFanArc"), (S.CtFanArc, "CtFanArc")):
+        g = cls()
+        for k, v in d[key].items():
+            if k != "source":
+                assert getattr(g, k) == pytest.approx(v), (key, k)
+    for cls, key in ((S.SinoFanArc.ge1, "SinoFanArc_ge1"), (S.CtFanArc.ge1, "CtFanArc_ge1")):
+        g = cls()
+        for k, v in d[key].items():
+            if k != "source":
+                assert getattr(g, k) == pytest.approx(v, rel=1e-6), (key, k)
+    assert S.SinoFanArc.short().na == 70
+    assert S.dims(S.CtFanFlat()) == (128, 64, 64)
+
+
+def test_plan_validation_without_gpu():
+    """Bad sizes are rejected on the host before any device work."""
+    with pytest.raises(S.SinogramsArgumentError):
+        S.fbp_sino_filter(np.ones((3, 40), np.float32), np.ones(32), extra=0)  # nb > npad, filter.jl:131
+
+
+def test_cases_match_reference_short_constructor():
+    g = C.short(dict(kind="arc", nb=128, d=1.0, offset=0.0, dsd=512.0), 128)
+    assert g["na"] == S.SinoFanArc.short().na
+    assert g["orbit"] == pytest.approx(S.SinoFanArc.short().orbit)
