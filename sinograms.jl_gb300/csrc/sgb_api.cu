@@ -7,6 +7,7 @@
 #include <vector>
 
 #include "sgb_common.cuh"
+#include "sgb_fdk_tma.cuh"
 #include "sgb_host.h"
 #include "sgb_kernels.cuh"
 
@@ -82,6 +83,12 @@ struct sgb_plan {
     float scale = 1.f;
     // staging for host-pointer calls
     DevBuf in_buf, filt_buf, img_buf;
+    // FDK back-projection: pitched filtered buffer and the TMA-staged kernel's set-up
+    int pitch = 0;
+    bool tma = false;
+    FdkTmaArgs targs{};
+    CUtensorMap tmap;
+    DevBuf flags;  // int[4]: box extents (pre-pass), error flags
     // optional stage timing
     bool timing = false;
     cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
@@ -143,6 +150,57 @@ int plan_image(sgb_plan *P, const sgb_image_geom *ig, double ds, int ndim, cudaS
     return upload_mask(ig->mask, (size_t)P->nx * P->ny * P->nz, P->mask, &P->mask_dev, st);
 }
 
+// Filtered-projection layout and back-projector choice for an FDK plan: rows padded to
+// a multiple of 8 samples (16-byte TMA strides for both storage types); the TMA-staged
+// kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.
+int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st) {
+    const sgb_ct_geom &g = P->cg;
+    const int elem = P->storage == SGB_STORE_BF16 ? 2 : 4;
+    P->pitch = (g.ns + 7) / 8 * 8;
+    SGB_TRY(P->filt_buf.reserve((size_t)P->pitch * g.nt * g.na * elem));
+    SGB_CUDA(cudaMemsetAsync(P->filt_buf.p, 0, (size_t)P->pitch * g.nt * g.na * elem, st));
+    SGB_TRY(P->flags.reserve(4 * sizeof(int)));
+    SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
+    FdkTmaArgs &A = P->targs;
+    A.trig = P->trig.as<float2>();
+    A.ns = g.ns;
+    A.nt = g.nt;
+    A.na = g.na;
+    A.nx = P->nx;
+    A.ny = P->ny;
+    A.nz = P->nz;
+    A.nv = g.na;
+    A.ia_skip = 1;
+    A.ws = (float)((g.ns + 1) / 2.0 + g.offset_s);
+    A.wt = (float)((g.nt + 1) / 2.0 + g.offset_t);
+    A.dsd_ds = (float)(g.dsd / g.ds);
+    A.dso_ds = (float)((g.dsd - g.dod) / g.ds);
+    A.inv_dtds = (float)(g.ds / g.dt);
+    auto start = [&](int i) { return ig->deltas[i] * (0 - ((ig->dims[i] - 1) / 2.0 + ig->offsets[i])) / g.ds; };
+    A.x0 = (float)start(0);
+    A.dx = (float)(ig->deltas[0] / g.ds);
+    A.y0 = (float)start(1);
+    A.dy = (float)(ig->deltas[1] / g.ds);
+    A.z0 = (float)start(2);
+    A.dz = (float)(ig->deltas[2] / g.ds);
+    A.is_arc = g.kind == SGB_ARC;
+    A.zu = 16;
+    A.elem_bytes = elem;
+    A.err = P->flags.as<int>() + 2;
+    // voxels must stay well inside the source circle for the corner bound to hold
+    double rx = std::fabs(ig->deltas[0]) * (ig->dims[0] / 2.0 + std::fabs(ig->offsets[0]) + 1);
+    double ry = std::fabs(ig->deltas[1]) * (ig->dims[1] / 2.0 + std::fabs(ig->offsets[1]) + 1);
+    P->tma = false;
+    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) {
+        SGB_TRY(fdk_tma_prepare(A, P->flags.as<int>(), st));
+        if (fdk_tma_usable(A)) {
+            SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &P->tmap));
+            P->tma = true;
+        }
+    }
+    return SGB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -178,6 +236,7 @@ int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_f
         P->sBj = 1;
         P->sBt = rg->ns;
     }
+    if (s == SGB_OK) s = plan_fdk_back(P, ig, st);
     if (s != SGB_OK) {
         delete P;
         return s;
@@ -250,6 +309,16 @@ int sgb_plan_destroy(sgb_plan *plan) {
     return SGB_OK;
 }
 
+int sgb_plan_info(const sgb_plan *P, int *info, int n) {
+    SGB_REQUIRE(P && info && n >= 5, "plan_info: bad argument");
+    info[0] = P->tma ? 1 : 0;
+    info[1] = P->targs.W;
+    info[2] = P->targs.H;
+    info[3] = P->pitch;
+    info[4] = P->targs.zu;
+    return SGB_OK;
+}
+
 int sgb_plan_set_timing(sgb_plan *P, int enable) {
     SGB_REQUIRE(P, "plan_set_timing: null plan");
     if (enable)
@@ -271,11 +340,12 @@ int sgb_plan_last_timing(sgb_plan *P, double *ms, int n) {
     return SGB_OK;
 }
 
-static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *out, cudaStream_t st) {
+static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *out, cudaStream_t st,
+                      int nout = 0) {
     FilterArgs A{};
     A.in = in_dev;
     A.ns = P->ndet;
-    A.nout = P->ndet;
+    A.nout = nout > 0 ? nout : P->ndet;
     A.nrows = nrows;
     A.nt = P->nrow;
     A.na = P->na;
@@ -298,10 +368,10 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     const size_t nproj = (size_t)g.ns * g.nt * g.na, nvox = (size_t)P->nx * P->ny * P->nz;
     const void *in_dev;
     SGB_TRY(stage_in(proj, nproj * sizeof(float), flags, P->in_buf, &in_dev, st));
-    SGB_TRY(P->filt_buf.reserve(nproj * (P->storage == SGB_STORE_BF16 ? 2 : 4)));
-    // step 1+2: view weights fused into the ramp filter (fdk.jl:72-75)
+    // step 1+2: view weights fused into the ramp filter (fdk.jl:72-75), rows padded to pitch
     P->mark(0, st);
-    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.nt * g.na, P->filt_buf.p, st));
+    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.nt * g.na, P->filt_buf.p, st,
+                       P->pitch));
     P->mark(1, st);
     float *img_dev = image;
     if (!(flags & SGB_DEVICE_PTRS)) {
@@ -309,6 +379,24 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
         img_dev = P->img_buf.as<float>();
     }
     // step 3: cbct_back (fdk.jl:78)
+    if (P->tma) {
+        FdkTmaArgs T = P->targs;
+        T.image = img_dev;
+        T.mask = P->mask_dev;
+        SGB_TRY(launch_fdk_tma(T, P->tmap, st));
+        P->mark(2, st);
+        if (!(flags & SGB_DEVICE_PTRS))
+            SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
+        SGB_TRY(finish(flags, st));
+        if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
+        int err = 0;
+        SGB_CUDA(cudaMemcpy(&err, P->targs.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) {
+            set_error("fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", err);
+            return (err & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
+        }
+        return SGB_OK;
+    }
     FdkArgs A{};
     A.proj = P->filt_buf.p;
     A.image = img_dev;
@@ -325,6 +413,7 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     A.nz = P->nz;
     A.nv = g.na;
     A.ia_skip = 1;
+    A.pitch = P->pitch;
     A.ws = (float)((g.ns + 1) / 2.0 + g.offset_s);
     A.wt = (float)((g.nt + 1) / 2.0 + g.offset_t);
     A.dsd_ds = (float)(g.dsd / g.ds);
@@ -464,6 +553,7 @@ int sgb_cbct_back(float *image, const float *proj, int ns, int nt, int na, const
     A.nz = nz;
     A.nv = (na + ia_skip - 1) / ia_skip;
     A.ia_skip = ia_skip;
+    A.pitch = ns;
     A.ws = (float)((ns + 1) / 2.0 + offset_s);  // cbct-back.jl:119-120
     A.wt = (float)((nt + 1) / 2.0 + offset_t);
     A.dsd_ds = (float)(dsd / ds);

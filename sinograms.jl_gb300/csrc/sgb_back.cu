@@ -48,7 +48,8 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
     }
     const int ns = A.ns, nt = A.nt;
     const float fns = (float)ns, fnt = (float)nt;
-    const long long view_stride = (long long)ns * nt;
+    const int pitch = A.pitch;
+    const long long view_stride = (long long)pitch * nt;
     const int tid = threadIdx.y * kBX + threadIdx.x;
 
     for (int v0 = 0; v0 < A.nv; v0 += kVChunk) {
@@ -84,9 +85,9 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
                 const float fit = floorf(bt);
                 if (fit >= 1.f && fit < fnt) {                       // :197 (t part)
                     const float ft = bt - fit;
-                    const TP *p = base + (long long)((int)fit - 1) * ns;
+                    const TP *p = base + (long long)((int)fit - 1) * pitch;
                     const float p00 = ld_proj(p), p10 = ld_proj(p + 1);
-                    const float p01 = ld_proj(p + ns), p11 = ld_proj(p + ns + 1);
+                    const float p01 = ld_proj(p + pitch), p11 = ld_proj(p + pitch + 1);
                     const float a0 = fmaf(fs, p10 - p00, p00);       // :205
                     const float a1 = fmaf(fs, p11 - p01, p01);       // :206
                     acc[k] = fmaf(w2, fmaf(ft, a1 - a0, a0), acc[k]); // :208

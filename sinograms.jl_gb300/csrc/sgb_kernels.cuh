@@ -36,6 +36,7 @@ struct FdkArgs {
     const float2 *trig;    // nv used views
     const float *xds, *yds, *zds;  // pixel centres / ds
     int ns, nt, na, nx, ny, nz, nv, ia_skip;
+    int pitch;             // row stride of proj in elements (>= ns)
     float ws, wt;          // (ns+1)/2 + offset_s, (nt+1)/2 + offset_t (1-based)
     float dsd_ds, dso_ds, inv_dtds;
     int is_arc;

@@ -48,15 +48,17 @@ __global__ void ellipse_sino_kernel(int kind, int nb, int na, const double *__re
 constexpr int kMaxEll = 64;
 
 // 3D: one CTA per (view, detector row block); per-view ellipsoid terms in shared memory.
-// For ellipsoid e with M = diag(1/radii) R^T: u0 = M (src - centre), v = M dir,
-// chord = 2 sqrt((u0.v)^2 - |v|^2 (|u0|^2 - 1)) / |v|^2.
+// For ellipsoid e with M = diag(1/radii) R^T, the ray src + l*dir is shifted to its
+// closest approach to the centre, q = (src - c) - ((src - c).dir) dir, so the FP32
+// quadratic has no cancellation: u = M q, v = M dir,
+// chord = 2 sqrt((u.v)^2 - |v|^2 (|u|^2 - 1)) / |v|^2.
 __global__ void ellipsoid_proj_kernel(int is_arc, int ns, int nt, int na, const double *__restrict__ s,
                                       const double *__restrict__ t, const double *__restrict__ beta,
                                       double dso, double dsd, const double *__restrict__ ell,
                                       int nell, float *proj) {
     __shared__ float sM[kMaxEll][9];
-    __shared__ float sU[kMaxEll][4];  // u0 and |u0|^2 - 1
-    __shared__ float sRho[kMaxEll];
+    __shared__ float sD[kMaxEll][4];  // src - centre (FP32 from FP64), density
+
     const int a = blockIdx.y;
     double sb, cb;
     sincos(beta[a], &sb, &cb);
@@ -70,17 +72,12 @@ __global__ void ellipsoid_proj_kernel(int is_arc, int ns, int nt, int na, const 
         double R[9] = {c1 * c2 * c3 - s1 * s3, -c1 * c2 * s3 - s1 * c3, c1 * s2,
                        s1 * c2 * c3 + c1 * s3, -s1 * c2 * s3 + c1 * c3, s1 * s2,
                        -s2 * c3,               s2 * s3,                 c2};
-        double d[3] = {src[0] - E[0], src[1] - E[1], src[2] - E[2]};
-        double uu = 0;
         for (int q = 0; q < 3; q++) {
             double inv = 1.0 / E[3 + q];
             for (int w = 0; w < 3; w++) sM[e][3 * q + w] = (float)(R[3 * w + q] * inv);
-            double u = (R[q] * d[0] + R[3 + q] * d[1] + R[6 + q] * d[2]) * inv;
-            sU[e][q] = (float)u;
-            uu += u * u;
+            sD[e][q] = (float)(src[q] - E[q]);
         }
-        sU[e][3] = (float)(uu - 1.0);
-        sRho[e] = (float)E[9];
+        sD[e][3] = (float)E[9];
     }
     __syncthreads();
     const int is = blockIdx.x * blockDim.x + threadIdx.x;
@@ -103,13 +100,19 @@ __global__ void ellipsoid_proj_kernel(int is_arc, int ns, int nt, int na, const 
         const float dx = dx0 * inv, dy = dy0 * inv, dz = dz0 * inv;
         float acc = 0.f;
         for (int e = 0; e < nell; e++) {
+            const float lam = sD[e][0] * dx + sD[e][1] * dy + sD[e][2] * dz;
+            const float qx = fmaf(-lam, dx, sD[e][0]), qy = fmaf(-lam, dy, sD[e][1]), qz = fmaf(-lam, dz, sD[e][2]);
+            const float u0 = sM[e][0] * qx + sM[e][1] * qy + sM[e][2] * qz;
+            const float u1 = sM[e][3] * qx + sM[e][4] * qy + sM[e][5] * qz;
+            const float u2 = sM[e][6] * qx + sM[e][7] * qy + sM[e][8] * qz;
             const float v0 = sM[e][0] * dx + sM[e][1] * dy + sM[e][2] * dz;
             const float v1 = sM[e][3] * dx + sM[e][4] * dy + sM[e][5] * dz;
             const float v2 = sM[e][6] * dx + sM[e][7] * dy + sM[e][8] * dz;
             const float vv = v0 * v0 + v1 * v1 + v2 * v2;
-            const float uv = sU[e][0] * v0 + sU[e][1] * v1 + sU[e][2] * v2;
-            const float disc = uv * uv - vv * sU[e][3];
-            if (disc > 0.f) acc += sRho[e] * 2.f * sqrtf(disc) / vv;
+            const float uv = u0 * v0 + u1 * v1 + u2 * v2;
+            const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+            const float disc = uv * uv - vv * (uu - 1.f);
+            if (disc > 0.f) acc += sD[e][3] * 2.f * sqrtf(disc) / vv;
         }
         proj[is + (long long)ns * (it + (long long)nt * a)] = acc;
     }

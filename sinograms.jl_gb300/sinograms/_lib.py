@@ -77,6 +77,7 @@ _SIGS = {
     "sgb_plan_destroy": (c_int, [P]),
     "sgb_plan_set_timing": (c_int, [P, c_int]),
     "sgb_plan_last_timing": (c_int, [P, P, c_int]),
+    "sgb_plan_info": (c_int, [P, P, c_int]),
 }
 
 _lib = None

@@ -70,6 +70,12 @@ class _Plan:
         """Record CUDA events around the filter and back-projection stages."""
         _status(_lib.lib().sgb_plan_set_timing(self._h, int(enable)), "plan_set_timing")
 
+    def info(self) -> dict:
+        """Execution layout: TMA-staged FDK kernel in use, staged box, row pitch, z-unroll."""
+        a = np.zeros(5, dtype=np.int32)
+        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 5), "plan_info")
+        return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]))
+
     def last_timing(self):
         """(filter_ms, back_ms) of the last fdk/fbp call (needs set_timing)."""
         ms = np.zeros(2)
