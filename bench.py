@@ -376,6 +376,25 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(args):
+    """Reduced profiling case (one GPU, a few launches): fdk of 512x512x64 voxels from
+    180 views of the benchmark geometry; the filtered projections (141 MB) exceed L2."""
+    import torch
+
+    import sinograms as S
+    g = dict(GEOM, na=180)
+    rg = S.CtFanFlat(**g)
+    ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
+    proj = S.ellipsoid_proj(rg, _phantom(), device=True)
+    plan = S.plan_fbp(rg, ig, storage=args.storage)
+    img = torch.empty((64, 512, 512), device="cuda")
+    for _ in range(2):
+        S.fdk(plan, proj, out=img)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "fdk_512x512x64_from_512x384x180", "storage": args.storage, **plan.info(),
+                      "mean_abs": float(img.abs().mean())}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -383,7 +402,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
+    ap.add_argument("--case", choices=["fdk-180v"], help="run the reduced profiling case instead")
+    ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
