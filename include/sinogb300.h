@@ -166,6 +166,18 @@ SGB_API int sgb_fbp_back_fan(float *image, const float *sino, int nb, int na, co
 SGB_API int sgb_bdd_project(const float *phantom, int nPix, int nDet, int na, const double *angle,
                     double DSD, double DS0, double pSize, double dSize, float *sino, int flags,
                     void *stream);
+/* No counterpart in the reference.  project_bdd for callers that cannot allocate device
+ * memory (services that forbid allocation after start-up, hosts whose device memory is
+ * owned by another allocator): phantom and sino are DEVICE pointers, angle is a host
+ * vector, and the per-view scratch lives in a 16 MiB array inside the library that each
+ * device holds until exit (requests needing more return SGB_ERR_ARG).  Nothing is
+ * allocated.  The work is enqueued on `stream` and the call returns without waiting.
+ * The first call on a device resolves the array's address and should come before any
+ * stream capture; calls on one device share the array, so calls whose GPU work
+ * overlaps race and must be serialised on one stream. */
+SGB_API int sgb_bdd_project_noalloc(const float *phantom, int nPix, int nDet, int na,
+                                    const double *angle, double DSD, double DS0, double pSize,
+                                    double dSize, float *sino, void *stream);
 /* backproject_bdd, src/sys2/bdd_2d.jl:119-220: sino (na, nDet) -> image (nPix,nPix). */
 SGB_API int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const double *angle,
                         double DSD, double DS0, double pSize, double dSize, float *image, int flags,

@@ -65,6 +65,8 @@ _SIGS = {
     "sgb_fbp_back_fan": (c_int, [P, P, c_int, c_int, P, P, c_double, c_double, c_double, c_int, c_double,
                                  c_float, P, P, c_int, c_int, P, c_int, c_int, P]),
     "sgb_bdd_project": (c_int, [P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P, c_int, P]),
+    "sgb_bdd_project_noalloc": (c_int, [P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P,
+                                        P]),
     "sgb_bdd_backproject": (c_int, [P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P, c_int,
                                     P]),
     "sgb_ellipse_sino": (c_int, [P, P, c_int, P, c_int, P]),
