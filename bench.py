@@ -223,11 +223,12 @@ def run_ours(args):
                      "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
                      "alg_bytes_per_launch": alg_bytes,
-                     "traffic": _traffic_from_profile("fdk_back_kernel_config3.md"),
+                     "traffic": _traffic_from_profile("fdk_tma_kernel_bench_dram.md"),
                      "fp32_issue": {"flops_per_update": F_UPD,
                                     "achieved_tflops": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12,
                                     "peak_tflops_nominal": NOMINAL_FP32_TFLOPS,
                                     "frac": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12 / NOMINAL_FP32_TFLOPS}},
+        "plan": forms[head]["plan"].info(),
         "gpu_launches": f["gpu_launches"],
         "clocks": f["clocks"],
     }

@@ -4,6 +4,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "sgb_common.cuh"
@@ -150,6 +152,84 @@ int plan_image(sgb_plan *P, const sgb_image_geom *ig, double ds, int ndim, cudaS
     return upload_mask(ig->mask, (size_t)P->nx * P->ny * P->nz, P->mask, &P->mask_dev, st);
 }
 
+// Autotuner of the TMA-staged back-projector: z-unroll candidates are sized by the
+// exhaustive box pre-pass, timed with CUDA events on the plan's own buffers (the kernel's
+// work does not depend on the data) and the fastest is kept.  Results are cached per
+// geometry so repeated plans of the same scan do not re-time.
+struct TuneKey {
+    int kind, ns, nt, na, nx, ny, nz, elem;
+    float dsd, dso, ds, dt, dx, dy, dz;
+    bool operator<(const TuneKey &o) const { return memcmp(this, &o, sizeof(TuneKey)) < 0; }
+};
+std::map<TuneKey, int> g_tune_cache;
+std::mutex g_tune_mu;
+
+int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
+    const sgb_ct_geom &g = P->cg;
+    FdkTmaArgs &A = P->targs;
+    TuneKey key;
+    memset(&key, 0, sizeof key);
+    key = TuneKey{g.kind, g.ns, g.nt, g.na, P->nx, P->ny, P->nz, A.elem_bytes, (float)g.dsd, (float)(g.dsd - g.dod),
+                  (float)g.ds, (float)g.dt, A.dx, A.dy, A.dz};
+    int best_zu = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) best_zu = it->second;
+    }
+    const long long updates = (long long)P->nx * P->ny * P->nz * g.na;
+    const int candidates[2] = {16, 32};
+    if (!best_zu) {
+        float best_ms = 1e30f;
+        cudaEvent_t e0, e1;
+        SGB_CUDA(cudaEventCreate(&e0));
+        SGB_CUDA(cudaEventCreate(&e1));
+        DevBuf img;
+        const bool time_it = updates > (1ll << 30);  // small problems: take the default
+        if (time_it) SGB_TRY(img.reserve((size_t)P->nx * P->ny * P->nz * sizeof(float)));
+        for (int zu : candidates) {
+            FdkTmaArgs T = A;
+            T.zu = zu;
+            SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
+            if (!fdk_tma_usable(T)) continue;
+            if (!time_it) {
+                best_zu = zu;
+                break;
+            }
+            CUtensorMap map;
+            SGB_TRY(fdk_tma_encode(T, P->filt_buf.p, P->pitch, &map));
+            T.image = img.as<float>();
+            T.mask = nullptr;
+            SGB_TRY(launch_fdk_tma(T, map, st));  // warm-up
+            SGB_CUDA(cudaEventRecord(e0, st));
+            SGB_TRY(launch_fdk_tma(T, map, st));
+            SGB_CUDA(cudaEventRecord(e1, st));
+            SGB_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            SGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_zu = zu;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
+        if (best_zu) {
+            std::lock_guard<std::mutex> lock(g_tune_mu);
+            g_tune_cache[key] = best_zu;
+        }
+    }
+    if (!best_zu) return SGB_OK;  // the direct kernel handles this geometry
+    A.zu = best_zu;
+    SGB_TRY(fdk_tma_prepare(A, P->flags.as<int>(), st));
+    if (!fdk_tma_usable(A)) return SGB_OK;
+    SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &P->tmap));
+    SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
+    P->tma = true;
+    return SGB_OK;
+}
+
 // Filtered-projection layout and back-projector choice for an FDK plan: rows padded to
 // a multiple of 8 samples (16-byte TMA strides for both storage types); the TMA-staged
 // kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.
@@ -191,13 +271,7 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st) {
     double rx = std::fabs(ig->deltas[0]) * (ig->dims[0] / 2.0 + std::fabs(ig->offsets[0]) + 1);
     double ry = std::fabs(ig->deltas[1]) * (ig->dims[1] / 2.0 + std::fabs(ig->offsets[1]) + 1);
     P->tma = false;
-    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) {
-        SGB_TRY(fdk_tma_prepare(A, P->flags.as<int>(), st));
-        if (fdk_tma_usable(A)) {
-            SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &P->tmap));
-            P->tma = true;
-        }
-    }
+    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) SGB_TRY(fdk_tma_autotune(P, st));
     return SGB_OK;
 }
 

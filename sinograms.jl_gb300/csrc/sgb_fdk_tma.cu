@@ -172,17 +172,19 @@ __device__ __forceinline__ float sload<__nv_bfloat16>(const __nv_bfloat16 *p) {
     return __bfloat162float(*p);
 }
 
-template <typename TP, bool ARC, int ZU, int VPS, int NSTAGE>
+template <typename TP, bool ARC, int ZU, int BW, int VPS, int NSTAGE>
 __global__ void __launch_bounds__(kThreads)
     fdk_tma_kernel(FdkTmaArgs A, const __grid_constant__ CUtensorMap map) {
     extern __shared__ __align__(128) unsigned char smraw[];
     // TMA destinations must be 128-byte aligned: align the dynamic region explicitly
     unsigned char *sm = smraw + ((128 - (smem_u32(smraw) & 127)) & 127);
-    const int W = A.W, H = A.H;
+    constexpr int W = BW;  // box row stride (samples); A.W == BW
+    const int H = A.H;
     const int box_bytes = A.box_bytes;  // W*H*sizeof(TP) rounded up to 128
     unsigned char *stage_base = sm;
     int2 *origin = reinterpret_cast<int2 *>(sm + (size_t)NSTAGE * VPS * box_bytes);  // [NSTAGE][VPS]
-    uint64_t *full = reinterpret_cast<uint64_t *>(origin + NSTAGE * VPS);
+    float2 *vtrig = reinterpret_cast<float2 *>(origin + NSTAGE * VPS);               // [NSTAGE][VPS]
+    uint64_t *full = reinterpret_cast<uint64_t *>(vtrig + NSTAGE * VPS);
     uint64_t *empty = full + NSTAGE;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -214,13 +216,15 @@ __global__ void __launch_bounds__(kThreads)
             if (lane < VPS) {
                 const int v = g * VPS + lane;
                 int2 o = make_int2(0, 0);
+                float2 sc = make_float2(0.f, 1.f);
                 if (v < A.nv) {
-                    const float2 sc = A.trig[v];
+                    sc = A.trig[v];
                     int s0, t0, w, h;
                     tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo, zhi, &s0, &t0, &w, &h);
                     o = make_int2(s0, t0);
                 }
                 origin[st * VPS + lane] = o;
+                vtrig[st * VPS + lane] = sc;
             }
             __syncwarp();
             if (lane == 0) {
@@ -260,15 +264,14 @@ __global__ void __launch_bounds__(kThreads)
         }
         const int nvalid = min(VPS, A.nv - g * VPS);
         for (int v = 0; v < nvalid; v++) {
-            const float2 sc = A.trig[g * VPS + v];
+            const float2 sc = vtrig[st * VPS + v];
             const int2 o = origin[st * VPS + v];
             const TP *box = reinterpret_cast<const TP *>(stage_base + (size_t)(st * VPS + v) * box_bytes);
             float bs, mag, w2;
             column_map<ARC>(A, x, y, sc.x, sc.y, &bs, &mag, &w2);
             const float fis = floorf(bs);
             if (!(fis >= 1.f && fis < (float)ns)) continue;  // cbct-back.jl:197 (s part)
-            const int is = (int)fis;
-            const int c = is - 1 - o.x;                        // box column of sample is-1
+            const int c = (int)fis - 1 - o.x;                  // box column of sample is-1
             if (c < 0 || c > W - 2) {
                 atomicOr(A.err, 1);
                 continue;
@@ -278,29 +281,48 @@ __global__ void __launch_bounds__(kThreads)
             const float bt0 = fmaf(magt, z0, A.wt), dbt = magt * A.dz;
             // rows usable: reference range [1, nt-1] intersected with the box
             const int lo = max(1, o.y + 1), hi = min(nt - 1, o.y + H - 1);
+            if (hi < lo) continue;
+            // rows of the first and last voxel bound the thread's rows (bt is monotone in k)
+            const float b_last = fmaf((float)(ZU - 1), dbt, bt0);
+            const int r0 = (int)floorf(clampf(fminf(bt0, b_last), -1e7f, 1e7f));
+            const int r1 = (int)floorf(clampf(fmaxf(bt0, b_last), -1e7f, 1e7f));
             {
                 // a reference-valid row outside the box would be an undersized box
-                const float b_first = bt0, b_last = fmaf((float)(ZU - 1), dbt, bt0);
-                const int r0 = (int)floorf(clampf(fminf(b_first, b_last), -1e7f, 1e7f));
-                const int r1 = (int)floorf(clampf(fmaxf(b_first, b_last), -1e7f, 1e7f));
                 const int v0 = max(1, r0), v1 = min(nt - 1, r1);
                 if (v0 <= v1 && (v0 < lo || v1 > hi)) atomicOr(A.err, 1);
             }
-            const TP *col = box + c - (o.y + 1) * W;  // row it (1-based) -> box row it-1-t0
+            const TP *base = box + c - (o.y + 1) * W;  // row it (1-based) -> box row it-1-t0
+            if (r0 >= lo && r1 <= hi) {
+                // every voxel of the column hits a valid, staged row: no per-voxel test
 #pragma unroll
-            for (int k = 0; k < ZU; k++) {
-                const float bt = fmaf((float)k, dbt, bt0);        // :189,192
-                const float fit = floorf(bt);
-                const int it = (int)fit;
-                if ((unsigned)(it - lo) <= (unsigned)(hi - lo)) {   // :197 (t part) and in-box
+                for (int k = 0; k < ZU; k++) {
+                    const float bt = fmaf((float)k, dbt, bt0);
+                    const float fit = floorf(bt);
+                    const TP *p = base + (int)fit * W;
                     const float ft = bt - fit;
-                    const TP *p = col + it * W;
                     const float p00 = sload(p), p10 = sload(p + 1);
                     const float p01 = sload(p + W), p11 = sload(p + W + 1);
-                    const float a0 = fmaf(fs, p10 - p00, p00);        // :205
-                    const float a1 = fmaf(fs, p11 - p01, p01);        // :206
-                    acc[k] = fmaf(w2, fmaf(ft, a1 - a0, a0), acc[k]);  // :208
+                    const float a0 = fmaf(fs, p10 - p00, p00);
+                    const float a1 = fmaf(fs, p11 - p01, p01);
+                    acc[k] = fmaf(w2, fmaf(ft, a1 - a0, a0), acc[k]);
                 }
+                continue;
+            }
+            const unsigned span = (unsigned)(hi - lo);
+#pragma unroll
+            for (int k = 0; k < ZU; k++) {
+                const float bt = fmaf((float)k, dbt, bt0);          // :189,192
+                const float fit = floorf(bt);
+                const int it = (int)fit;
+                const bool ok = (unsigned)(it - lo) <= span;          // :197 (t part) and in-box
+                const TP *p = base + (ok ? it : lo) * W;              // dropped taps read a safe row
+                const float wk = ok ? w2 : 0.f;
+                const float ft = bt - fit;
+                const float p00 = sload(p), p10 = sload(p + 1);
+                const float p01 = sload(p + W), p11 = sload(p + W + 1);
+                const float a0 = fmaf(fs, p10 - p00, p00);          // :205
+                const float a1 = fmaf(fs, p11 - p01, p01);          // :206
+                acc[k] = fmaf(wk, fmaf(ft, a1 - a0, a0), acc[k]);   // :208
             }
         }
         __syncwarp();
@@ -334,20 +356,27 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 constexpr int kVPS = 4, kNStage = 4;
 
-template <typename TP, bool ARC, int ZU>
-int launch_t(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+template <typename TP, bool ARC, int ZU, int BW>
+int launch_w(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
     dim3 grid(floor_div_up(A.nx, kTX), floor_div_up(A.ny, kTY), floor_div_up(A.nz, ZU));
     size_t smem = fdk_tma_smem(A, kVPS, kNStage);
-    auto k = fdk_tma_kernel<TP, ARC, ZU, kVPS, kNStage>;
+    auto k = fdk_tma_kernel<TP, ARC, ZU, BW, kVPS, kNStage>;
     SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<grid, kThreads, smem, st>>>(A, map);
     return after_launch("fdk_tma_kernel");
 }
 
+template <typename TP, bool ARC, int ZU>
+int launch_t(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+    if (A.W == 32) return launch_w<TP, ARC, ZU, 32>(A, map, st);
+    return launch_w<TP, ARC, ZU, 64>(A, map, st);
+}
+
 }  // namespace
 
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage) {
-    return 128 + (size_t)nstage * vps * A.box_bytes + sizeof(int2) * nstage * vps + 2 * sizeof(uint64_t) * nstage;
+    return 128 + (size_t)nstage * vps * A.box_bytes + (sizeof(int2) + sizeof(float2)) * nstage * vps +
+           2 * sizeof(uint64_t) * nstage;
 }
 
 int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st) {
@@ -368,14 +397,14 @@ int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st) {
     int ext[2];
     SGB_CUDA(cudaMemcpyAsync(ext, ext_dev, sizeof ext, cudaMemcpyDeviceToHost, st));
     SGB_CUDA(cudaStreamSynchronize(st));
-    A.W = (ext[0] + A.align - 1) / A.align * A.align;
+    A.W = ext[0] <= 32 ? 32 : (ext[0] <= 64 ? 64 : ext[0]);  // compile-time widths 32 and 64
     A.H = ext[1];
     A.box_bytes = (int)(((size_t)A.W * A.H * A.elem_bytes + 127) / 128 * 128);
     return SGB_OK;
 }
 
 bool fdk_tma_usable(const FdkTmaArgs &A) {
-    if (A.W <= 0 || A.H <= 1 || A.W > 256 || A.H > 256) return false;
+    if (A.W > 64 || A.H <= 1 || A.H > 256) return false;
     if (fdk_tma_smem(A, kVPS, kNStage) > 200 * 1024) return false;
     return encode_fn() != nullptr;
 }
