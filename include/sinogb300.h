@@ -220,6 +220,26 @@ SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
  * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z. */
 SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
 
+/* ------------------------------------------------------------ batched FDK */
+/* No counterpart in the reference (it reconstructs one scan per fdk call,
+ * src/fbp3/fdk.jl:65-81): up to 64 independent CtFanArc/CtFanFlat scans of different sizes
+ * reconstructed by one CUDA graph (every scan's weighted filter, then ONE persistent
+ * back-projection launch over a longest-first work queue of voxel tiles).  Each scan
+ * gets the FDK of its own plan_fbp.  The batch owns the device input/output buffers. */
+typedef struct sgb_batch sgb_batch;
+SGB_API int sgb_batch_fdk_create(int nscans, const sgb_ct_geom *rgs, const sgb_image_geom *igs,
+                                 const sgb_filter_opts *opt, sgb_batch **batch);
+/* Copy scan i's projections (ns,nt,na) in / its image (nx,ny,nz) out (host or device). */
+SGB_API int sgb_batch_fdk_set_input(sgb_batch *batch, int i, const float *proj, int flags, void *stream);
+SGB_API int sgb_batch_fdk_get_output(sgb_batch *batch, int i, float *image, int flags, void *stream);
+/* Device addresses of scan i's input and output buffers (zero-copy producers/consumers). */
+SGB_API int sgb_batch_fdk_buffers(sgb_batch *batch, int i, float **proj_dev, float **image_dev);
+/* fdk of every scan (one graph launch on `stream`). */
+SGB_API int sgb_batch_fdk_run(sgb_batch *batch, int flags, void *stream);
+/* *updates = total voxel-view updates; info = {nscans, work items, persistent CTAs, box width}. */
+SGB_API int sgb_batch_fdk_info(const sgb_batch *batch, long long *updates, int *info, int n);
+SGB_API int sgb_batch_fdk_destroy(sgb_batch *batch);
+
 #ifdef __cplusplus
 }
 #endif

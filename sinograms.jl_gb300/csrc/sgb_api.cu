@@ -164,7 +164,7 @@ struct TuneKey {
 std::map<TuneKey, int> g_tune_cache;
 std::mutex g_tune_mu;
 
-int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
+int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
     const sgb_ct_geom &g = P->cg;
     FdkTmaArgs &A = P->targs;
     TuneKey key;
@@ -179,6 +179,7 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
     }
     const long long updates = (long long)P->nx * P->ny * P->nz * g.na;
     const int candidates[2] = {16, 32};
+    if (!tune) best_zu = 16;
     if (!best_zu) {
         float best_ms = 1e30f;
         cudaEvent_t e0, e1;
@@ -191,7 +192,7 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
             FdkTmaArgs T = A;
             T.zu = zu;
             SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
-            if (!fdk_tma_usable(T)) continue;
+            if (!fdk_tma_choose(T)) continue;
             if (!time_it) {
                 best_zu = zu;
                 break;
@@ -223,7 +224,7 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
     if (!best_zu) return SGB_OK;  // the direct kernel handles this geometry
     A.zu = best_zu;
     SGB_TRY(fdk_tma_prepare(A, P->flags.as<int>(), st));
-    if (!fdk_tma_usable(A)) return SGB_OK;
+    if (!fdk_tma_choose(A)) return SGB_OK;
     SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &P->tmap));
     SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
     P->tma = true;
@@ -233,7 +234,7 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st) {
 // Filtered-projection layout and back-projector choice for an FDK plan: rows padded to
 // a multiple of 8 samples (16-byte TMA strides for both storage types); the TMA-staged
 // kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.
-int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st) {
+int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool tune) {
     const sgb_ct_geom &g = P->cg;
     const int elem = P->storage == SGB_STORE_BF16 ? 2 : 4;
     P->pitch = (g.ns + 7) / 8 * 8;
@@ -271,7 +272,7 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st) {
     double rx = std::fabs(ig->deltas[0]) * (ig->dims[0] / 2.0 + std::fabs(ig->offsets[0]) + 1);
     double ry = std::fabs(ig->deltas[1]) * (ig->dims[1] / 2.0 + std::fabs(ig->offsets[1]) + 1);
     P->tma = false;
-    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) SGB_TRY(fdk_tma_autotune(P, st));
+    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) SGB_TRY(fdk_tma_autotune(P, st, tune));
     return SGB_OK;
 }
 
@@ -281,8 +282,16 @@ extern "C" {
 
 // ----------------------------------------------------------------------- plans
 
+static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
+                          bool tune, sgb_plan **plan);
+
 int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
                     sgb_plan **plan) {
+    return create_ct_plan(rg, ig, opt, true, plan);
+}
+
+static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
+                          bool tune, sgb_plan **plan) {
     SGB_REQUIRE(rg && ig && plan, "plan_fbp: null argument");
     SGB_REQUIRE(rg->kind == SGB_ARC || rg->kind == SGB_FLAT, "plan_fbp: CtGeom must be CtFanArc or CtFanFlat");
     SGB_REQUIRE(rg->ns > 1 && rg->nt > 1 && rg->na > 1, "plan_fbp: ns, nt, na must exceed 1");
@@ -310,7 +319,7 @@ int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_f
         P->sBj = 1;
         P->sBt = rg->ns;
     }
-    if (s == SGB_OK) s = plan_fdk_back(P, ig, st);
+    if (s == SGB_OK) s = plan_fdk_back(P, ig, st, tune);
     if (s != SGB_OK) {
         delete P;
         return s;
@@ -748,6 +757,194 @@ int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const dou
                         double DSD, double DS0, double pSize, double dSize, float *image, int flags,
                         void *stream) {
     return bdd_seam(false, sino, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, image, flags, stream);
+}
+
+// ------------------------------------------------------------------ batched FDK
+
+}  // extern "C"
+
+struct sgb_batch {
+    std::vector<sgb_plan *> plans;
+    DevBuf scans, work, counter, flags;
+    FdkBatchArgs args{};
+    FdkBatchMaps maps;
+    long long updates = 0;
+    int nctas = 0;
+    cudaStream_t capture = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~sgb_batch() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (capture) cudaStreamDestroy(capture);
+        for (auto *p : plans) delete p;
+    }
+};
+
+namespace {
+
+int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geom *igs, const sgb_filter_opts *opt) {
+    cudaStream_t st = 0;
+    int W = 32, box_bytes = 0, elem = 4;
+    for (int i = 0; i < n; i++) {
+        sgb_plan *P = nullptr;
+        SGB_TRY(create_ct_plan(rgs + i, igs + i, opt, false, &P));
+        B->plans.push_back(P);
+        if (!P->tma) {
+            set_error("batch_fdk: scan %d does not fit the TMA-staged back-projector (voxels too close to the "
+                      "source or detector box too wide); reconstruct it with its own plan",
+                      i);
+            return SGB_ERR_UNSUPPORTED;
+        }
+        const sgb_ct_geom &g = P->cg;
+        SGB_TRY(P->in_buf.reserve((size_t)g.ns * g.nt * g.na * sizeof(float)));
+        SGB_TRY(P->img_buf.reserve((size_t)P->nx * P->ny * P->nz * sizeof(float)));
+        W = std::max(W, P->targs.W);
+        elem = P->targs.elem_bytes;
+        B->updates += (long long)P->nx * P->ny * P->nz * g.na;
+    }
+    SGB_TRY(B->flags.reserve(4 * sizeof(int)));
+    SGB_CUDA(cudaMemsetAsync(B->flags.p, 0, 4 * sizeof(int), st));
+    SGB_TRY(B->counter.reserve(sizeof(int)));
+    // common box width, per-scan tensor maps, device argument table
+    std::vector<FdkTmaArgs> scans(n);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) {
+        sgb_plan *P = B->plans[i];
+        FdkTmaArgs A = P->targs;
+        A.W = W;
+        A.box_bytes = (int)(((size_t)W * A.H * A.elem_bytes + 127) / 128 * 128);
+        A.image = P->img_buf.as<float>();
+        A.mask = P->mask_dev;
+        A.err = B->flags.as<int>();
+        SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &B->maps.m[i]));
+        box_bytes = std::max(box_bytes, A.box_bytes);
+        scans[i] = A;
+        order[i] = i;
+    }
+    SGB_TRY(upload_raw(scans.data(), sizeof(FdkTmaArgs) * n, B->scans, st));
+    // work list: scans with more views first (longer tiles), tiles in order
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return scans[a].nv > scans[b].nv; });
+    std::vector<int2> work;
+    for (int i : order) {
+        const FdkTmaArgs &A = scans[i];
+        const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
+        for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
+    }
+    SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
+    FdkBatchArgs &BA = B->args;
+    BA.scans = B->scans.as<FdkTmaArgs>();
+    BA.work = B->work.as<int2>();
+    BA.counter = B->counter.as<int>();
+    BA.err = B->flags.as<int>();
+    BA.nscans = n;
+    BA.nwork = (int)work.size();
+    BA.W = W;
+    BA.box_bytes = box_bytes;
+    BA.elem_bytes = elem;
+    BA.vps = 4;
+    if (fdk_batch_smem(BA) > 200 * 1024) BA.vps = 2;
+    SGB_REQUIRE(fdk_batch_smem(BA) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
+    int dev = 0, nsm = 0;
+    SGB_CUDA(cudaGetDevice(&dev));
+    SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const int per = fdk_batch_ctas_per_sm(BA);
+    SGB_REQUIRE(per > 0, "batch_fdk: the persistent kernel cannot be resident");
+    B->nctas = nsm * per;
+    // one CUDA graph: every scan's weighted filter, then the persistent back-projection
+    SGB_CUDA(cudaStreamCreateWithFlags(&B->capture, cudaStreamNonBlocking));
+    SGB_CUDA(cudaStreamBeginCapture(B->capture, cudaStreamCaptureModeRelaxed));
+    int s = SGB_OK;
+    for (int i = 0; i < n && s == SGB_OK; i++) {
+        sgb_plan *P = B->plans[i];
+        s = run_filter(P, P->in_buf.as<float>(), (long long)P->cg.nt * P->cg.na, P->filt_buf.p, B->capture, P->pitch);
+    }
+    if (s == SGB_OK && cudaMemsetAsync(BA.counter, 0, sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
+    if (s == SGB_OK) s = launch_fdk_batch(BA, B->maps, B->nctas, B->capture);
+    cudaError_t e = cudaStreamEndCapture(B->capture, &B->graph);
+    if (s != SGB_OK) return s;
+    if (e != cudaSuccess) {
+        set_error("batch_fdk: graph capture failed: %s", cudaGetErrorString(e));
+        return SGB_ERR_CUDA;
+    }
+    SGB_CUDA(cudaGraphInstantiate(&B->exec, B->graph, 0));
+    return SGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sgb_batch_fdk_create(int n, const sgb_ct_geom *rgs, const sgb_image_geom *igs, const sgb_filter_opts *opt,
+                         sgb_batch **out) {
+    SGB_REQUIRE(rgs && igs && out, "batch_fdk_create: null argument");
+    SGB_REQUIRE(n >= 1 && n <= kMaxBatch, "batch_fdk_create: 1 <= nscans <= %d", kMaxBatch);
+    sgb_batch *B = new sgb_batch();
+    int s = batch_build(B, n, rgs, igs, opt);
+    if (s != SGB_OK) {
+        delete B;
+        return s;
+    }
+    *out = B;
+    return SGB_OK;
+}
+
+int sgb_batch_fdk_set_input(sgb_batch *B, int i, const float *proj, int flags, void *stream) {
+    SGB_REQUIRE(B && proj && i >= 0 && i < (int)B->plans.size(), "batch_fdk_set_input: bad argument");
+    sgb_plan *P = B->plans[i];
+    const size_t bytes = (size_t)P->cg.ns * P->cg.nt * P->cg.na * sizeof(float);
+    SGB_CUDA(cudaMemcpyAsync(P->in_buf.p, proj, bytes,
+                             (flags & SGB_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             as_stream(stream)));
+    return finish(flags, as_stream(stream));
+}
+
+int sgb_batch_fdk_get_output(sgb_batch *B, int i, float *image, int flags, void *stream) {
+    SGB_REQUIRE(B && image && i >= 0 && i < (int)B->plans.size(), "batch_fdk_get_output: bad argument");
+    sgb_plan *P = B->plans[i];
+    const size_t bytes = (size_t)P->nx * P->ny * P->nz * sizeof(float);
+    SGB_CUDA(cudaMemcpyAsync(image, P->img_buf.p, bytes,
+                             (flags & SGB_DEVICE_PTRS) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             as_stream(stream)));
+    return finish(flags, as_stream(stream));
+}
+
+int sgb_batch_fdk_buffers(sgb_batch *B, int i, float **proj_dev, float **image_dev) {
+    SGB_REQUIRE(B && proj_dev && image_dev && i >= 0 && i < (int)B->plans.size(), "batch_fdk_buffers: bad argument");
+    *proj_dev = B->plans[i]->in_buf.as<float>();
+    *image_dev = B->plans[i]->img_buf.as<float>();
+    return SGB_OK;
+}
+
+int sgb_batch_fdk_run(sgb_batch *B, int flags, void *stream) {
+    SGB_REQUIRE(B && B->exec, "batch_fdk_run: bad batch");
+    cudaStream_t st = as_stream(stream);
+    SGB_CUDA(cudaGraphLaunch(B->exec, st));
+    g_launches.fetch_add((long long)B->plans.size() + 1, std::memory_order_relaxed);
+    if (flags & SGB_ASYNC) return SGB_OK;
+    SGB_CUDA(cudaStreamSynchronize(st));
+    int err = 0;
+    SGB_CUDA(cudaMemcpy(&err, B->args.err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        set_error("batch_fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", err);
+        return (err & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
+    }
+    return SGB_OK;
+}
+
+int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n) {
+    SGB_REQUIRE(B && updates && info && n >= 4, "batch_fdk_info: bad argument");
+    *updates = B->updates;
+    info[0] = (int)B->plans.size();
+    info[1] = B->args.nwork;
+    info[2] = B->nctas;
+    info[3] = B->args.W;
+    return SGB_OK;
+}
+
+int sgb_batch_fdk_destroy(sgb_batch *B) {
+    delete B;
+    return SGB_OK;
 }
 
 int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nell, float *sino, int flags,

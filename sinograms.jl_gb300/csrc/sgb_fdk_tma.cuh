@@ -19,11 +19,34 @@ struct FdkTmaArgs {
     int elem_bytes;         // 4 (fp32) or 2 (bf16) filtered projections
     int align;              // TMA x-coordinate alignment in elements
     int W, H, box_bytes;    // staged box (samples) and its shared-memory footprint
+    int vps;                // views per pipeline stage (4, or 2 for large boxes)
 };
+
+// Batched persistent back-projection: per-scan arguments in device memory, tensor maps in
+// the kernel parameter block (at most kMaxBatch scans per launch).
+constexpr int kMaxBatch = 64;
+struct FdkBatchMaps {
+    CUtensorMap m[kMaxBatch];
+};
+struct FdkBatchArgs {
+    const FdkTmaArgs *scans;  // device array [nscans]
+    const int2 *work;         // device array [nwork]: (scan, tile) in execution order
+    int *counter;             // device work counter (zero before the launch)
+    int *err;                 // device error flags
+    int nscans, nwork;
+    int W;                    // common compile-time box width (32 or 64)
+    int box_bytes;            // largest box of the batch
+    int elem_bytes;
+    int vps;                  // views per pipeline stage (4 or 2)
+};
+size_t fdk_batch_smem(const FdkBatchArgs &B);
+int fdk_batch_ctas_per_sm(const FdkBatchArgs &B);
+int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
 
 // Sizes the detector box over every (tile, view) of the geometry (device pre-pass).
 int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st);
-bool fdk_tma_usable(const FdkTmaArgs &A);
+// Picks views-per-stage for the staged box; false when no ring fits shared memory.
+bool fdk_tma_choose(FdkTmaArgs &A);
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage);
 // 3D tensor map over the filtered projections (pitch, nt, na).
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map);

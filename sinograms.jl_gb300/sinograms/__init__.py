@@ -11,7 +11,7 @@ from .filters import (SinogramsArgumentError, Window, _angle_weights, fbp_filter
                       ramp_arc, ramp_flat)
 from .geom import (CtFanArc, CtFanFlat, ImageGeom, SinoFanArc, SinoFanFlat, SinoPar, _ar, _dso, _gamma, _gamma_max,
                    _orbit_short, _rfov, _s, _t, angles, axes, dims, downsample)
-from .phantoms import ellipse_sino, ellipsoid_proj, random_ellipses, random_ellipsoids
-from .recon import FBPNormalPlan, FDKplan, cbct_back, fbp, fbp_back, fdk, plan_fbp
+from .phantoms import ellipse_sino, ellipsoid_proj, random_ct_scans, random_ellipses, random_ellipsoids
+from .recon import FBPNormalPlan, FDKBatch, FDKplan, cbct_back, fbp, fbp_back, fdk, plan_fbp
 
 __all__ = [n for n in dir() if not n.startswith("__")]

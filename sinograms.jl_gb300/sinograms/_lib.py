@@ -80,6 +80,13 @@ _SIGS = {
     "sgb_plan_set_timing": (c_int, [P, c_int]),
     "sgb_plan_last_timing": (c_int, [P, P, c_int]),
     "sgb_plan_info": (c_int, [P, P, c_int]),
+    "sgb_batch_fdk_create": (c_int, [c_int, P, P, P, P]),
+    "sgb_batch_fdk_set_input": (c_int, [P, c_int, P, c_int, P]),
+    "sgb_batch_fdk_get_output": (c_int, [P, c_int, P, c_int, P]),
+    "sgb_batch_fdk_buffers": (c_int, [P, c_int, P, P]),
+    "sgb_batch_fdk_run": (c_int, [P, c_int, P]),
+    "sgb_batch_fdk_info": (c_int, [P, P, P, c_int]),
+    "sgb_batch_fdk_destroy": (c_int, [P]),
 }
 
 _lib = None

@@ -65,3 +65,31 @@ def random_ellipsoids(n: int, seed: int, rmax: float, zmax: float, axes=(3.0, 60
     return np.stack([r * np.cos(t), r * np.sin(t), rng.uniform(-zmax, zmax, n), rng.uniform(*axes, n),
                      rng.uniform(*axes, n), rng.uniform(*axes, n), rng.uniform(0, 2 * math.pi, n),
                      np.arccos(rng.uniform(-1, 1, n)), rng.uniform(0, 2 * math.pi, n), rng.uniform(*dens, n)], axis=1)
+
+
+def random_ct_scans(n: int, seed: int, nell: int = 30):
+    """n seeded CBCT scans of uneven size (the batched-FDK workload): CtFanFlat or CtFanArc
+    50/50, nx = ny in {128..384 step 32}, nz in {128..256 step 32}, na U{180..720},
+    ns U{256..768}, nt U{128..384}, dsd U[800,1200], dso = 0.6 dsd, ds = dt = 1; voxels
+    sized so the xy square is inscribed in the radial FOV and the slab spans 90% of the
+    axial FOV; each scan gets its own random-ellipsoid phantom scaled to its FOV.
+    Returns (geometries, image geometries, ellipsoid tables)."""
+    from .geom import CtFanArc, CtFanFlat, ImageGeom, _rfov
+    rng = np.random.default_rng(seed)
+    rgs, igs, ells = [], [], []
+    for i in range(n):
+        cls = CtFanArc if rng.random() < 0.5 else CtFanFlat
+        nx = int(rng.choice(np.arange(128, 385, 32)))
+        nz = int(rng.choice(np.arange(128, 257, 32)))
+        na, ns, nt = int(rng.integers(180, 721)), int(rng.integers(256, 769)), int(rng.integers(128, 385))
+        dsd = float(rng.uniform(800, 1200))
+        rg = cls(ns=ns, nt=nt, ds=1.0, dt=1.0, na=na, dsd=dsd, dod=0.4 * dsd)
+        rf = _rfov(rg)
+        zfov = 0.6 * nt  # dso/dsd * nt * dt (ct-geom.jl:250)
+        dx = 2 * rf / (math.sqrt(2) * nx)
+        dz = 0.9 * zfov / nz
+        rgs.append(rg)
+        igs.append(ImageGeom((nx, nx, nz), (dx, dx, dz)))
+        e = random_ellipsoids(nell, seed * 1000 + i, 0.6 * rf, 0.35 * nz * dz, axes=(0.02 * rf, 0.3 * rf))
+        ells.append(e)
+    return rgs, igs, ells

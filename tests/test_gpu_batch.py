@@ -1,0 +1,72 @@
+"""Batched FDK (one CUDA graph, one persistent back-projection launch over many scans):
+every scan must equal its own single-scan plan and the FP64 oracle."""
+import numpy as np
+import pytest
+
+import cases as C
+import oracle as O
+import sinograms as S
+
+pytestmark = pytest.mark.gpu
+
+
+def _scans():
+    rgs = [S.CtFanFlat(ns=61, nt=40, ds=1.0, dt=1.1, na=37, dsd=220.0, dod=70.0, offset_s=0.25),
+           S.CtFanArc(ns=48, nt=32, ds=1.2, dt=1.0, na=24, dsd=180.0, dod=60.0),
+           S.CtFanArc.short(ns=40, nt=24, ds=1.0, dt=1.0, na=30, dsd=150.0, dod=50.0),
+           S.CtFanFlat(ns=80, nt=20, ds=0.9, dt=1.3, na=50, dsd=300.0, dod=100.0, offset_t=-0.5),
+           S.CtFanFlat(ns=33, nt=30, ds=1.0, dt=1.0, na=19, dsd=140.0, dod=40.0)]
+    igs = [S.ImageGeom((21, 19, 13), (1.0, 1.0, 1.1), (0.3, 0.0, 0.0)),
+           S.ImageGeom((32, 32, 16), (1.1, 1.1, 1.0)),
+           S.ImageGeom((18, 18, 9), (1.0, 1.0, 1.0)),
+           S.ImageGeom((40, 24, 11), (1.0, 1.0, 1.0)),
+           S.ImageGeom((16, 17, 20), (0.9, 0.9, 0.8))]
+    ig3 = igs[3]
+    igs[3] = ig3.with_mask(ig3.circle(10.0))
+    return rgs, igs
+
+
+def _oracle_geom(rg):
+    return dict(kind=rg.kind, ns=rg.ns, nt=rg.nt, ds=rg.ds, dt=rg.dt, offset_s=rg.offset_s, offset_t=rg.offset_t,
+                na=rg.na, orbit=rg.orbit, orbit_start=rg.orbit_start, source_offset=0.0, dsd=rg.dsd, dod=rg.dod)
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_batch_equals_single_scan_plans(cuda, storage):
+    rgs, igs = _scans()
+    batch = S.FDKBatch(rgs, igs, storage=storage)
+    info = batch.info()
+    assert info["scans"] == len(rgs) and info["ctas"] > 0
+    projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
+    for i, p in enumerate(projs):
+        batch.set_input(i, p)
+    for rep in range(2):  # the graph replays
+        batch.run()
+        for i, (rg, ig, p) in enumerate(zip(rgs, igs, projs)):
+            out = batch.get_output(i)
+            single = S.fdk(S.plan_fbp(rg, ig, storage=storage), p)
+            err = O.rel_rmse(out, single)
+            assert err < 1e-5, (i, rep, err)
+            if ig.mask is not None:
+                assert np.all(out[~ig.mask] == 0)
+
+
+def test_batch_against_oracle(cuda):
+    rgs, igs = _scans()
+    batch = S.FDKBatch(rgs, igs)
+    projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
+    for i, p in enumerate(projs):
+        batch.set_input(i, p)
+    batch.run()
+    for i, (rg, ig, p) in enumerate(zip(rgs, igs, projs)):
+        ref = O.fdk(_oracle_geom(rg), dict(dims=ig.dims, deltas=ig.deltas, offsets=ig.offsets, mask=ig.mask), p)
+        out = batch.get_output(i)
+        assert O.rel_rmse(out, ref) < 1e-5, i
+        assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max(), i
+
+
+def test_batch_rejects_too_many_scans():
+    rgs = [S.CtFanFlat(ns=16, nt=8, na=8)] * 65
+    igs = [S.ImageGeom((8, 8, 4))] * 65
+    with pytest.raises(S.SinogramsArgumentError):
+        S.FDKBatch(rgs, igs)
