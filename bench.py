@@ -276,10 +276,12 @@ def measure_batched(args):
     batch.run()  # synchronous run: checks the kernel's error flags
     ms = e0.elapsed_time(e1) / args.steps
     info = batch.info()
+    stages = batch.timing()
     return {"workload": "fdk_batch_48_uneven_scans_seed4", "value": info["updates"] / (ms / 1e3), "unit": UNIT,
             "ms_per_run": ms, "updates_per_run": info["updates"], "scans": info["scans"],
-            "work_items": info["work_items"], "persistent_ctas": info["ctas"], "box_width": info["box_width"],
-            "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps}
+            "work_items": info["work_items"], "persistent_ctas": info["ctas"], "persistent_launches": info["launches"],
+            "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps,
+            "stage_ms": {"filters": stages[0], "back_by_box_class": stages[1:]}}
 
 
 # --------------------------------------------------------------------- CPU side
@@ -414,12 +416,29 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch_case(args):
+    """Profiling case for the batched workload: build the 48-scan batch, run it twice."""
+    import torch
+
+    import sinograms as S
+    rgs, igs, ells = S.random_ct_scans(48, 4)
+    batch = S.FDKBatch(rgs, igs)
+    for i, (rg, e) in enumerate(zip(rgs, ells)):
+        batch.set_input(i, S.ellipsoid_proj(rg, e, device=True))
+    for _ in range(2):
+        batch.run()
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "fdk_batch_48_uneven_scans_seed4", **batch.info(), "stage_ms": batch.timing()}))
+
+
 def run_case(args):
     """Reduced profiling case (one GPU, a few launches): fdk of 512x512x64 voxels from
     180 views of the benchmark geometry; the filtered projections (141 MB) exceed L2."""
     import torch
 
     import sinograms as S
+    if args.case == "fdk-batch":
+        return run_batch_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -441,7 +460,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
-    ap.add_argument("--case", choices=["fdk-180v"], help="run the reduced profiling case instead")
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch"], help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
     args = ap.parse_args()
     if args.case:

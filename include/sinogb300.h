@@ -236,8 +236,11 @@ SGB_API int sgb_batch_fdk_get_output(sgb_batch *batch, int i, float *image, int 
 SGB_API int sgb_batch_fdk_buffers(sgb_batch *batch, int i, float **proj_dev, float **image_dev);
 /* fdk of every scan (one graph launch on `stream`). */
 SGB_API int sgb_batch_fdk_run(sgb_batch *batch, int flags, void *stream);
-/* *updates = total voxel-view updates; info = {nscans, work items, persistent CTAs, box width}. */
+/* *updates = total voxel-view updates; info = {nscans, work items, persistent CTAs of the
+ * first launch, number of persistent launches (one per detector-box width class)}. */
 SGB_API int sgb_batch_fdk_info(const sgb_batch *batch, long long *updates, int *info, int n);
+/* Stage times of the last run (ms): [0] all weighted filters, [1..] each persistent launch. */
+SGB_API int sgb_batch_fdk_timing(sgb_batch *batch, double *ms, int n);
 SGB_API int sgb_batch_fdk_destroy(sgb_batch *batch);
 
 #ifdef __cplusplus

@@ -766,14 +766,19 @@ int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const dou
 struct sgb_batch {
     std::vector<sgb_plan *> plans;
     DevBuf scans, work, counter, flags;
-    FdkBatchArgs args{};
+    std::vector<FdkBatchArgs> classes;  // one persistent launch per box-width class
+    std::vector<int> class_ctas;
+    FdkBatchArgs args{};                // totals for sgb_batch_fdk_info
     FdkBatchMaps maps;
     long long updates = 0;
     int nctas = 0;
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    cudaEvent_t ev[6] = {};  // graph event nodes: start, filters done, each class done
     ~sgb_batch() {
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
         if (capture) cudaStreamDestroy(capture);
@@ -785,7 +790,7 @@ namespace {
 
 int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geom *igs, const sgb_filter_opts *opt) {
     cudaStream_t st = 0;
-    int W = 32, box_bytes = 0, elem = 4;
+    int elem = 4;
     for (int i = 0; i < n; i++) {
         sgb_plan *P = nullptr;
         SGB_TRY(create_ct_plan(rgs + i, igs + i, opt, false, &P));
@@ -799,68 +804,92 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         const sgb_ct_geom &g = P->cg;
         SGB_TRY(P->in_buf.reserve((size_t)g.ns * g.nt * g.na * sizeof(float)));
         SGB_TRY(P->img_buf.reserve((size_t)P->nx * P->ny * P->nz * sizeof(float)));
-        W = std::max(W, P->targs.W);
         elem = P->targs.elem_bytes;
         B->updates += (long long)P->nx * P->ny * P->nz * g.na;
     }
     SGB_TRY(B->flags.reserve(4 * sizeof(int)));
     SGB_CUDA(cudaMemsetAsync(B->flags.p, 0, 4 * sizeof(int), st));
-    SGB_TRY(B->counter.reserve(sizeof(int)));
-    // common box width, per-scan tensor maps, device argument table
+    SGB_TRY(B->counter.reserve(4 * sizeof(int)));
+    // per-scan tensor maps (each with its own box width) and device argument table
     std::vector<FdkTmaArgs> scans(n);
-    std::vector<int> order(n);
     for (int i = 0; i < n; i++) {
         sgb_plan *P = B->plans[i];
         FdkTmaArgs A = P->targs;
-        A.W = W;
-        A.box_bytes = (int)(((size_t)W * A.H * A.elem_bytes + 127) / 128 * 128);
         A.image = P->img_buf.as<float>();
         A.mask = P->mask_dev;
         A.err = B->flags.as<int>();
         SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &B->maps.m[i]));
-        box_bytes = std::max(box_bytes, A.box_bytes);
         scans[i] = A;
-        order[i] = i;
     }
     SGB_TRY(upload_raw(scans.data(), sizeof(FdkTmaArgs) * n, B->scans, st));
-    // work list: scans with more views first (longer tiles), tiles in order
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return scans[a].nv > scans[b].nv; });
+    // box-width classes (32/64/128): each is one persistent launch over a longest-first
+    // work list of its scans' voxel tiles, so fine scans keep small boxes
     std::vector<int2> work;
-    for (int i : order) {
-        const FdkTmaArgs &A = scans[i];
-        const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
-        for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
-    }
-    SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
-    FdkBatchArgs &BA = B->args;
-    BA.scans = B->scans.as<FdkTmaArgs>();
-    BA.work = B->work.as<int2>();
-    BA.counter = B->counter.as<int>();
-    BA.err = B->flags.as<int>();
-    BA.nscans = n;
-    BA.nwork = (int)work.size();
-    BA.W = W;
-    BA.box_bytes = box_bytes;
-    BA.elem_bytes = elem;
-    BA.vps = 4;
-    if (fdk_batch_smem(BA) > 200 * 1024) BA.vps = 2;
-    SGB_REQUIRE(fdk_batch_smem(BA) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
     int dev = 0, nsm = 0;
     SGB_CUDA(cudaGetDevice(&dev));
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const int per = fdk_batch_ctas_per_sm(BA);
-    SGB_REQUIRE(per > 0, "batch_fdk: the persistent kernel cannot be resident");
-    B->nctas = nsm * per;
-    // one CUDA graph: every scan's weighted filter, then the persistent back-projection
+    std::vector<size_t> class_begin;
+    for (int W : {32, 64, 128}) {
+        std::vector<int> order;
+        int box_bytes = 0;
+        for (int i = 0; i < n; i++)
+            if (scans[i].W == W) {
+                order.push_back(i);
+                box_bytes = std::max(box_bytes, scans[i].box_bytes);
+            }
+        if (order.empty()) continue;
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return scans[a].nv > scans[b].nv; });
+        FdkBatchArgs C{};
+        C.nscans = n;
+        C.W = W;
+        C.box_bytes = box_bytes;
+        C.elem_bytes = elem;
+        C.vps = 4;
+        if (fdk_batch_smem(C) > 200 * 1024) C.vps = 2;
+        if (fdk_batch_smem(C) > 200 * 1024) C.vps = 1;
+        SGB_REQUIRE(fdk_batch_smem(C) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
+        class_begin.push_back(work.size());
+        for (int i : order) {
+            const FdkTmaArgs &A = scans[i];
+            const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
+            for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
+        }
+        C.nwork = (int)(work.size() - class_begin.back());
+        B->classes.push_back(C);
+    }
+    SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
+    SGB_REQUIRE(B->classes.size() <= 4, "batch_fdk: too many box classes");
+    for (size_t c = 0; c < B->classes.size(); c++) {
+        FdkBatchArgs &C = B->classes[c];
+        C.scans = B->scans.as<FdkTmaArgs>();
+        C.work = B->work.as<int2>() + class_begin[c];
+        C.counter = B->counter.as<int>() + c;
+        C.err = B->flags.as<int>();
+        const int per = fdk_batch_ctas_per_sm(C);
+        SGB_REQUIRE(per > 0, "batch_fdk: the persistent kernel cannot be resident");
+        B->class_ctas.push_back(nsm * per);
+    }
+    B->args = B->classes.front();
+    B->args.nwork = (int)work.size();
+    B->nctas = B->class_ctas.front();
+    // one CUDA graph: every scan's weighted filter, then the persistent back-projection(s)
+    for (size_t i = 0; i < 2 + B->classes.size(); i++) SGB_CUDA(cudaEventCreate(&B->ev[i]));
     SGB_CUDA(cudaStreamCreateWithFlags(&B->capture, cudaStreamNonBlocking));
     SGB_CUDA(cudaStreamBeginCapture(B->capture, cudaStreamCaptureModeRelaxed));
     int s = SGB_OK;
+    if (cudaEventRecordWithFlags(B->ev[0], B->capture, cudaEventRecordExternal) != cudaSuccess) s = SGB_ERR_CUDA;
     for (int i = 0; i < n && s == SGB_OK; i++) {
         sgb_plan *P = B->plans[i];
         s = run_filter(P, P->in_buf.as<float>(), (long long)P->cg.nt * P->cg.na, P->filt_buf.p, B->capture, P->pitch);
     }
-    if (s == SGB_OK && cudaMemsetAsync(BA.counter, 0, sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
-    if (s == SGB_OK) s = launch_fdk_batch(BA, B->maps, B->nctas, B->capture);
+    if (s == SGB_OK && cudaMemsetAsync(B->counter.p, 0, 4 * sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
+    if (s == SGB_OK && cudaEventRecordWithFlags(B->ev[1], B->capture, cudaEventRecordExternal) != cudaSuccess)
+        s = SGB_ERR_CUDA;
+    for (size_t c = 0; c < B->classes.size() && s == SGB_OK; c++) {
+        s = launch_fdk_batch(B->classes[c], B->maps, B->class_ctas[c], B->capture);
+        if (s == SGB_OK && cudaEventRecordWithFlags(B->ev[2 + c], B->capture, cudaEventRecordExternal) != cudaSuccess)
+            s = SGB_ERR_CUDA;
+    }
     cudaError_t e = cudaStreamEndCapture(B->capture, &B->graph);
     if (s != SGB_OK) return s;
     if (e != cudaSuccess) {
@@ -920,7 +949,7 @@ int sgb_batch_fdk_run(sgb_batch *B, int flags, void *stream) {
     SGB_REQUIRE(B && B->exec, "batch_fdk_run: bad batch");
     cudaStream_t st = as_stream(stream);
     SGB_CUDA(cudaGraphLaunch(B->exec, st));
-    g_launches.fetch_add((long long)B->plans.size() + 1, std::memory_order_relaxed);
+    g_launches.fetch_add((long long)(B->plans.size() + B->classes.size()), std::memory_order_relaxed);
     if (flags & SGB_ASYNC) return SGB_OK;
     SGB_CUDA(cudaStreamSynchronize(st));
     int err = 0;
@@ -938,7 +967,21 @@ int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n)
     info[0] = (int)B->plans.size();
     info[1] = B->args.nwork;
     info[2] = B->nctas;
-    info[3] = B->args.W;
+    info[3] = (int)B->classes.size();
+    return SGB_OK;
+}
+
+int sgb_batch_fdk_timing(sgb_batch *B, double *ms, int n) {
+    SGB_REQUIRE(B && ms && n >= 1 + (int)B->classes.size(), "batch_fdk_timing: bad argument");
+    const size_t last = 1 + B->classes.size();
+    SGB_CUDA(cudaEventSynchronize(B->ev[last]));
+    float t;
+    SGB_CUDA(cudaEventElapsedTime(&t, B->ev[0], B->ev[1]));
+    ms[0] = t;
+    for (size_t c = 0; c < B->classes.size(); c++) {
+        SGB_CUDA(cudaEventElapsedTime(&t, B->ev[1 + c], B->ev[2 + c]));
+        ms[1 + c] = t;
+    }
     return SGB_OK;
 }
 

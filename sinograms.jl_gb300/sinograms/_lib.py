@@ -86,6 +86,7 @@ _SIGS = {
     "sgb_batch_fdk_buffers": (c_int, [P, c_int, P, P]),
     "sgb_batch_fdk_run": (c_int, [P, c_int, P]),
     "sgb_batch_fdk_info": (c_int, [P, P, P, c_int]),
+    "sgb_batch_fdk_timing": (c_int, [P, P, c_int]),
     "sgb_batch_fdk_destroy": (c_int, [P]),
 }
 

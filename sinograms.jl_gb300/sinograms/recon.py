@@ -273,8 +273,15 @@ class FDKBatch:
             st = None
         _status(_lib.lib().sgb_batch_fdk_run(self._h, 0 if sync else _lib.SGB_ASYNC, st), "batch_fdk_run")
 
+    def timing(self):
+        """Stage times (ms) of the last run: weighted filters, then each persistent launch."""
+        n = 1 + self.info()["launches"]
+        ms = np.zeros(n)
+        _status(_lib.lib().sgb_batch_fdk_timing(self._h, ptr(ms), n), "batch_fdk_timing")
+        return [float(v) for v in ms]
+
     def info(self) -> dict:
         u = ctypes.c_longlong()
         a = np.zeros(4, dtype=np.int32)
         _status(_lib.lib().sgb_batch_fdk_info(self._h, ctypes.byref(u), ptr(a), 4), "batch_fdk_info")
-        return dict(updates=int(u.value), scans=int(a[0]), work_items=int(a[1]), ctas=int(a[2]), box_width=int(a[3]))
+        return dict(updates=int(u.value), scans=int(a[0]), work_items=int(a[1]), ctas=int(a[2]), launches=int(a[3]))
