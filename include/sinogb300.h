@@ -192,6 +192,10 @@ SGB_API int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nel
                      void *stream);
 SGB_API int sgb_ellipsoid_proj(const sgb_ct_geom *rg, const double *ell, int nell, float *proj, int flags,
                        void *stream);
+/* Pixel image (nx, ny) of ellipses on a 2D ImageGeom, averaged over sub x sub samples per
+ * pixel (the phantoms of the learned-filter training set). */
+SGB_API int sgb_ellipse_image(const sgb_image_geom *ig, const double *ell, int nell, int sub,
+                              float *image, int flags, void *stream);
 
 /* ------------------------------------------------------------------ plans */
 /* plan_fbp(rg::CtGeom, ig), src/fbp3/plan3.jl:60-72 (FDKplan). */
@@ -208,6 +212,13 @@ SGB_API int sgb_fdk(sgb_plan *plan, const float *proj, float *image, int flags, 
  * sino (nb, na, nslices) -> image (nx, ny, nslices). */
 SGB_API int sgb_fbp(sgb_plan *plan, const float *sino, float *image, int nslices, int flags,
             void *stream);
+/* The two stages of fbp(plan, sino) (fbp.jl:72-86) for a 2D plan: view weights + ramp
+ * filter (fbp_sino_filter), and the plan's back-projector (fbp_back) on filtered rows.
+ * Shapes as sgb_fbp; filtered is (nb, na, nslices). */
+SGB_API int sgb_fbp_filter_rows(sgb_plan *plan, const float *sino, float *filtered, int nslices,
+                                int flags, void *stream);
+SGB_API int sgb_fbp_backproject(sgb_plan *plan, const float *filtered, float *image, int nslices,
+                                int flags, void *stream);
 SGB_API int sgb_plan_destroy(sgb_plan *plan);
 /* Stage timing (no counterpart in the reference): when enabled, fdk/fbp record CUDA
  * events on the call's stream around the filter and back-projection kernels;
@@ -219,6 +230,29 @@ SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
  * back-projection uses the TMA-staged kernel, info[1..2] = staged box (samples),
  * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z. */
 SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
+
+/* ------------------------------------------------------- learned filter */
+/* No counterpart in the reference.  A per-row 1D CNN (5 conv layers, kernel 9, 32
+ * channels, GELU; BF16 weights, FP32 master copy and accumulation) applied to
+ * ramp-filtered detector rows z as a learned residual, y = z + scale * net(z / scale):
+ * it stands in for the apodizing window of fbp_filter (src/fbp/window.jl).  Rows are
+ * (rows, L) with L detector samples; at most 65535 rows per call.  params (nparam FP32
+ * values, layer by layer: W (cout,cin,9) then b) may be NULL for a seeded He init with a
+ * zero last layer (an untrained filter is the plain ramp). */
+typedef struct sgb_lf sgb_lf;
+SGB_API int sgb_lf_create(float scale, const float *params, unsigned long long seed, sgb_lf **lf);
+SGB_API int sgb_lf_num_params(const sgb_lf *lf);
+SGB_API int sgb_lf_get_params(const sgb_lf *lf, float *params, float *scale);
+/* y = z + scale * net(z/scale) */
+SGB_API int sgb_lf_apply(sgb_lf *lf, const float *z, long long rows, int L, float *y, int flags,
+                         void *stream);
+/* loss = mean((z + scale*net(z/scale) - target)^2) / scale^2; grads (nparam) optional */
+SGB_API int sgb_lf_loss_grad(sgb_lf *lf, const float *z, const float *target, long long rows, int L,
+                             double *loss, float *grads, int flags, void *stream);
+/* one Adam step (lr; beta 0.9/0.999) on the batch; *loss (optional) is the pre-step loss */
+SGB_API int sgb_lf_train_step(sgb_lf *lf, const float *z, const float *target, long long rows, int L,
+                              float lr, double *loss, int flags, void *stream);
+SGB_API int sgb_lf_destroy(sgb_lf *lf);
 
 /* ------------------------------------------------------------ batched FDK */
 /* No counterpart in the reference (it reconstructs one scan per fdk call,

@@ -556,6 +556,64 @@ int sgb_fbp(sgb_plan *P, const float *sino, float *image, int nslices, int flags
     return finish(flags, st);
 }
 
+// Stages of fbp(plan, sino): the plan's weights + ramp filter, and its back-projector.
+int sgb_fbp_filter_rows(sgb_plan *P, const float *sino, float *filtered, int nslices, int flags, void *stream) {
+    SGB_REQUIRE(P && sino && filtered && nslices >= 1, "fbp_filter_rows: bad argument");
+    SGB_REQUIRE(!P->ct, "fbp_filter_rows: needs a 2D plan");
+    cudaStream_t st = as_stream(stream);
+    const sgb_sino_geom &g = P->sg;
+    const size_t n = (size_t)g.nb * g.na * nslices;
+    const void *in_dev;
+    SGB_TRY(stage_in(sino, n * sizeof(float), flags, P->in_buf, &in_dev, st));
+    float *out_dev = filtered;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->filt_buf.reserve(n * sizeof(float)));
+        out_dev = P->filt_buf.as<float>();
+    }
+    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.na * nslices, out_dev, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(filtered, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return finish(flags, st);
+}
+
+int sgb_fbp_backproject(sgb_plan *P, const float *filtered, float *image, int nslices, int flags, void *stream) {
+    SGB_REQUIRE(P && filtered && image && nslices >= 1, "fbp_backproject: bad argument");
+    SGB_REQUIRE(!P->ct, "fbp_backproject: needs a 2D plan");
+    cudaStream_t st = as_stream(stream);
+    const sgb_sino_geom &g = P->sg;
+    const size_t n = (size_t)g.nb * g.na * nslices, npix = (size_t)P->nx * P->ny * nslices;
+    const void *in_dev;
+    SGB_TRY(stage_in(filtered, n * sizeof(float), flags, P->in_buf, &in_dev, st));
+    float *img_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->img_buf.reserve(npix * sizeof(float)));
+        img_dev = P->img_buf.as<float>();
+    }
+    Back2Args A{};
+    A.sino = static_cast<const float *>(in_dev);
+    A.image = img_dev;
+    A.mask = P->mask_dev;
+    A.trig = P->trig.as<float2>();
+    A.xds = P->xds.as<float>();
+    A.yds = P->yds.as<float>();
+    A.nb = g.nb;
+    A.na = g.na;
+    A.nx = P->nx;
+    A.ny = P->ny;
+    A.nv = g.na;
+    A.ia_skip = 1;
+    A.nslices = nslices;
+    A.wb = (float)((g.nb + 1) / 2.0 + g.offset);
+    A.mode = g.kind;
+    A.dsd_ds = (float)(g.dsd / g.d);
+    A.dso_ds = (float)((g.dsd - g.dod) / g.d);
+    A.so_ds = (float)(g.source_offset / g.d);
+    SGB_TRY(launch_back2(A, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, img_dev, npix * sizeof(float), cudaMemcpyDeviceToHost, st));
+    return finish(flags, st);
+}
+
 // ----------------------------------------------------------------------- seams
 
 int sgb_fbp_sino_filter(const float *in, int nb, long long nrows, const double *Hk, int npad,
@@ -1010,6 +1068,26 @@ int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nell, float
                                 rg->dsd - rg->dod, rg->dsd, de.as<double>(), nell, out_dev, st));
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(sino, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int sgb_ellipse_image(const sgb_image_geom *ig, const double *ell, int nell, int sub, float *image, int flags,
+                      void *stream) {
+    SGB_REQUIRE(ig && ell && image && nell >= 0 && sub >= 1 && ig->ndim == 2, "ellipse_image: bad argument");
+    cudaStream_t st = as_stream(stream);
+    DevBuf de, dout;
+    SGB_TRY(upload_f64(ell, (size_t)6 * std::max(nell, 1), de, st));
+    size_t n = (size_t)ig->dims[0] * ig->dims[1];
+    float *out_dev = image;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(dout.reserve(n * sizeof(float)));
+        out_dev = dout.as<float>();
+    }
+    SGB_TRY(launch_ellipse_image(ig->dims[0], ig->dims[1], ig->deltas[0], ig->deltas[1], ig->offsets[0],
+                                 ig->offsets[1], de.as<double>(), nell, sub, out_dev, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
     SGB_CUDA(cudaStreamSynchronize(st));
     return SGB_OK;
 }

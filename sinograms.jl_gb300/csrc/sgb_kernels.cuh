@@ -73,6 +73,8 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
                     cudaStream_t st);
 
 // -------------------------------------------------------- analytic phantoms
+int launch_ellipse_image(int nx, int ny, double dx, double dy, double ox, double oy, const double *ell_dev,
+                         int nell, int sub, float *img, cudaStream_t st);
 int launch_ellipse_sino(int kind, int nb, int na, const double *s_dev, const double *beta_dev,
                         double dso, double dsd, const double *ell_dev, int nell, float *sino,
                         cudaStream_t st);

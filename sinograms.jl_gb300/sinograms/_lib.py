@@ -71,6 +71,9 @@ _SIGS = {
                                     P]),
     "sgb_ellipse_sino": (c_int, [P, P, c_int, P, c_int, P]),
     "sgb_ellipsoid_proj": (c_int, [P, P, c_int, P, c_int, P]),
+    "sgb_ellipse_image": (c_int, [P, P, c_int, c_int, P, c_int, P]),
+    "sgb_fbp_filter_rows": (c_int, [P, P, P, c_int, c_int, P]),
+    "sgb_fbp_backproject": (c_int, [P, P, P, c_int, c_int, P]),
     "sgb_plan_fbp_ct": (c_int, [P, P, P, P]),
     "sgb_plan_fbp_sino": (c_int, [P, P, P, P]),
     "sgb_plan_filter": (c_int, [P, P, P]),
@@ -80,6 +83,13 @@ _SIGS = {
     "sgb_plan_set_timing": (c_int, [P, c_int]),
     "sgb_plan_last_timing": (c_int, [P, P, c_int]),
     "sgb_plan_info": (c_int, [P, P, c_int]),
+    "sgb_lf_create": (c_int, [c_float, P, ctypes.c_ulonglong, P]),
+    "sgb_lf_num_params": (c_int, [P]),
+    "sgb_lf_get_params": (c_int, [P, P, P]),
+    "sgb_lf_apply": (c_int, [P, P, c_ll, c_int, P, c_int, P]),
+    "sgb_lf_loss_grad": (c_int, [P, P, P, c_ll, c_int, P, P, c_int, P]),
+    "sgb_lf_train_step": (c_int, [P, P, P, c_ll, c_int, c_float, P, c_int, P]),
+    "sgb_lf_destroy": (c_int, [P]),
     "sgb_batch_fdk_create": (c_int, [c_int, P, P, P, P]),
     "sgb_batch_fdk_set_input": (c_int, [P, c_int, P, c_int, P]),
     "sgb_batch_fdk_get_output": (c_int, [P, c_int, P, c_int, P]),

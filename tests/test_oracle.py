@@ -174,3 +174,17 @@ def test_oracle_fp32_build_close_to_fp64():
     f = np.load(os.path.join(HERE, "golden", "fdk_flat.npz"))
     r32 = O.fdk(c["rg"], c["ig"], f["proj"], bits=32)
     assert O.rel_rmse(r32, f["ref"]) < 1e-5
+
+
+def test_learned_oracle_gradient_finite_differences():
+    """The FP64 network restatement's analytic gradient matches central differences."""
+    import learned_oracle as LO
+    rng = np.random.default_rng(11)
+    p = 0.3 * rng.standard_normal(LO.nparams())
+    z, t = rng.standard_normal((3, 20)), rng.standard_normal((3, 20))
+    loss, g = LO.loss_grad(p, z, t, 0.7, bf16_weights=False)
+    for i in rng.choice(p.size, 25, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-5
+        fd = (LO.loss_grad(p + e, z, t, 0.7, False)[0] - LO.loss_grad(p - e, z, t, 0.7, False)[0]) / 2e-5
+        assert fd == pytest.approx(g[i], rel=1e-6, abs=1e-9 * np.abs(g).max())
