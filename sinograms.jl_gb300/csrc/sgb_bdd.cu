@@ -8,11 +8,13 @@
 // The pixel grid of the reference is a set of x boundaries and y row centres
 // (:32-35), so for both mapping axes the mapped boundaries of one image "row" are an
 // affine function of the pixel index: rowm[c] = r0 + c * delta.  The kernels use that
-// closed form instead of a table.  Interpolating the prefix integral at a mapped
-// point is then  F(u) = delta * (S[c] + f * val[c])  with q = (u - r0)/delta,
-// c = floor(q), f = q - c, S the exclusive prefix sum of the row -- a warp-level scan.
-// Prefix sums and F are carried in FP64 because the result is a difference of two
-// nearly equal prefix values; data and accumulations stay FP32.
+// closed form instead of a table.  The interpolated prefix integral of a row at a mapped
+// point is F(q) = delta * (sum_{c<floor q} val[c] + frac(q) val[floor q]), q = (u-r0)/delta,
+// clamped to [0, nPix] (Flat extrapolation).  The reference's |diff| of F at consecutive
+// boundaries is evaluated as a local sum over the few pixels (or detector bins) between
+// them plus the two fractional end terms: exactly the same quantity, and accurate in FP32
+// because no large prefix values are subtracted.  FP64 is kept for the per-view and
+// per-row geometry (trig, boundary mapping); the per-sample work is FP32.
 //
 // Quirks kept: detector y offset -(DSD-DS0) - dSize/2 (:29), Flat extrapolation,
 // |diff| (the pair is not linear for signed images), the (na, nDet) sinogram layout,
@@ -91,135 +93,97 @@ __device__ __forceinline__ void row_affine(const ViewInfo &vi, int r, int nPix, 
 }
 
 // ------------------------------------------------------------ per-view set-up
-// forward: info, detm (nDet+1), L (nDet).  back: info, knots kn and prefix kv over the
-// detector (ascending knots: reversed when detm descends, :198-202).
-__global__ void bdd_setup_kernel(BddArgs G, ViewInfo *info, double *detm, double *L,
-                                 const float *sino, double *kn, double *kv) {
+// forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info, ascending knots K
+// (nDet+1), per-bin integrals B (nDet, ascending order: sino * L * |ddetm|, signed as the
+// reference's prefix, :196) and 1/(K[j+1]-K[j]) (reversed when detm descends, :198-202).
+__global__ void bdd_setup_kernel(BddArgs G, ViewInfo *info, float *detm, float *L, const float *sino, float *kn,
+                                 float *kb, float *kinv) {
     const int p = blockIdx.x, nDet = G.nDet;
     const double beta = G.angle[p];
     const ViewInfo vi = view_info(beta, G.DS0);
     if (threadIdx.x == 0) info[p] = vi;
-    double *dm = detm + (size_t)p * (nDet + 1);
-    for (int k = threadIdx.x; k <= nDet; k += blockDim.x)
-        dm[k] = det_boundary(vi, beta, k, nDet, G.DSD, G.DS0, G.dSize);
-    __syncthreads();
     if (!sino) {
-        for (int n = threadIdx.x; n < nDet; n += blockDim.x)
-            L[(size_t)p * nDet + n] = det_scale(vi, dm[n], dm[n + 1], G.pSize);
+        float *dm = detm + (size_t)p * (nDet + 1);
+        for (int k = threadIdx.x; k <= nDet; k += blockDim.x)
+            dm[k] = (float)det_boundary(vi, beta, k, nDet, G.DSD, G.DS0, G.dSize);
+        for (int n = threadIdx.x; n < nDet; n += blockDim.x) {
+            const double d0 = det_boundary(vi, beta, n, nDet, G.DSD, G.DS0, G.dSize);
+            const double d1 = det_boundary(vi, beta, n + 1, nDet, G.DSD, G.DS0, G.dSize);
+            L[(size_t)p * nDet + n] = (float)det_scale(vi, d0, d1, G.pSize);
+        }
         return;
     }
-    // back: Ppj[n+1] = sum_{n'<=n} sino[p,n'] * L[n'] * (detm[n'+1]-detm[n']) (:196)
-    __shared__ double chunk[kThreads];
-    const int per = (nDet + blockDim.x - 1) / blockDim.x;
-    const int n0 = threadIdx.x * per, n1 = min(nDet, n0 + per);
-    double s = 0;
-    for (int n = n0; n < n1; n++) {
-        double l = det_scale(vi, dm[n], dm[n + 1], G.pSize);
-        s += ((double)sino[p + (size_t)G.na * n] * l) * (dm[n + 1] - dm[n]);
+    const double d_first = det_boundary(vi, beta, 0, nDet, G.DSD, G.DS0, G.dSize);
+    const double d_second = det_boundary(vi, beta, 1, nDet, G.DSD, G.DS0, G.dSize);
+    const bool desc = d_first > d_second;
+    float *K = kn + (size_t)p * (nDet + 1), *B = kb + (size_t)p * nDet, *KI = kinv + (size_t)p * nDet;
+    for (int k = threadIdx.x; k <= nDet; k += blockDim.x) {
+        const int src = desc ? nDet - k : k;
+        K[k] = (float)det_boundary(vi, beta, src, nDet, G.DSD, G.DS0, G.dSize);
     }
-    chunk[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {  // exclusive scan of kThreads chunk sums
-        double run = 0;
-        for (int i = 0; i < (int)blockDim.x; i++) {
-            double c = chunk[i];
-            chunk[i] = run;
-            run += c;
-        }
-    }
-    __syncthreads();
-    const bool desc = dm[0] > dm[1];
-    double *K = kn + (size_t)p * (nDet + 1), *V = kv + (size_t)p * (nDet + 1);
-    double run = chunk[threadIdx.x];
-    if (threadIdx.x == 0) {
-        K[desc ? nDet : 0] = dm[0];
-        V[desc ? nDet : 0] = 0.0;
-    }
-    for (int n = n0; n < n1; n++) {
-        double l = det_scale(vi, dm[n], dm[n + 1], G.pSize);
-        run += ((double)sino[p + (size_t)G.na * n] * l) * (dm[n + 1] - dm[n]);
-        int k = n + 1, slot = desc ? nDet - k : k;
-        K[slot] = dm[k];
-        V[slot] = run;
+    for (int j = threadIdx.x; j < nDet; j += blockDim.x) {
+        // ascending bin j covers reference bin n = desc ? nDet-1-j : j
+        const int n = desc ? nDet - 1 - j : j;
+        const double d0 = det_boundary(vi, beta, n, nDet, G.DSD, G.DS0, G.dSize);
+        const double d1 = det_boundary(vi, beta, n + 1, nDet, G.DSD, G.DS0, G.dSize);
+        const double w = ((double)sino[p + (size_t)G.na * n] * det_scale(vi, d0, d1, G.pSize)) * (d1 - d0);
+        B[j] = (float)(desc ? -w : w);  // integral over the bin in the ascending direction
+        KI[j] = (float)(1.0 / std::fabs(d1 - d0));
     }
 }
 
-// warp exclusive prefix sum (FP64) of the row values into S[0..nPix]
-__device__ __forceinline__ void warp_prefix(const float *val, int nPix, double *S, int lane) {
-    const int per = (nPix + 31) / 32;
-    const int c0 = lane * per, c1 = min(nPix, c0 + per);
-    double s = 0;
-    for (int c = c0; c < c1; c++) s += (double)val[c];
-    double incl = s;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        double t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    double run = __shfl_up_sync(0xffffffffu, incl, 1);
-    if (lane == 0) run = 0.0;
-    for (int c = c0; c < c1; c++) {
-        S[c] = run;
-        run += (double)val[c];
-    }
-    if (lane == 31) S[nPix] = incl;
-}
-
-// integral of the mapped row up to u (interp of Ppj with Flat extrapolation, :98)
-__device__ __forceinline__ double row_integral(double u, double r0, double delta, const double *S,
-                                               const float *val, int nPix) {
-    double q = (u - r0) / delta;
-    if (!(q > 0)) return 0.0;
-    if (q >= nPix) return S[nPix] * delta;
-    int c = (int)q;
-    double f = q - c;
-    return (S[c] + f * (double)val[c]) * delta;
+// |F(hi) - F(lo)| / delta for a row: local sum of val over [lo, hi] in pixel units,
+// lo, hi clamped to [0, nPix]; val has nPix+1 entries (the last one zero).
+__device__ __forceinline__ float row_span(const float *val, int nPix, float q0, float q1) {
+    float lo = fminf(q0, q1), hi = fmaxf(q0, q1);
+    lo = fminf(fmaxf(lo, 0.f), (float)nPix);
+    hi = fminf(fmaxf(hi, 0.f), (float)nPix);
+    const int c0 = (int)lo, c1 = (int)hi;
+    float s = (hi - c1) * val[c1] - (lo - c0) * val[c0];
+    for (int c = c0; c < c1; c++) s += val[c];
+    return s;
 }
 
 // ------------------------------------------------------------------ forward
 __global__ void __launch_bounds__(kThreads)
-    bdd_project_kernel(BddArgs G, const ViewInfo *info, const double *detm, const double *L,
+    bdd_project_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L,
                        const float *__restrict__ phantom, float *sino, int rows_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet, p = blockIdx.x;
-    double *dm = reinterpret_cast<double *>(smraw);                 // nDet+1
-    double *Sall = dm + (nDet + 1);                                 // kWarps x (nPix+1)
-    float *tile = reinterpret_cast<float *>(Sall + kWarps * (nPix + 1));  // kWarps x nPix
-    float *accw = tile + kWarps * nPix;                             // kWarps x nDet
+    float *dm = reinterpret_cast<float *>(smraw);   // nDet+1
+    float *tile = dm + (nDet + 1);                    // kWarps x (nPix+1)
+    float *accw = tile + kWarps * (nPix + 1);         // kWarps x nDet
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const ViewInfo vi = info[p];
     for (int k = threadIdx.x; k <= nDet; k += kThreads) dm[k] = detm[(size_t)p * (nDet + 1) + k];
     for (int i = threadIdx.x; i < kWarps * nDet; i += kThreads) accw[i] = 0.f;
-    double *S = Sall + warp * (nPix + 1);
-    float *val = tile + warp * nPix;
+    float *val = tile + warp * (nPix + 1);
     float *acc = accw + warp * nDet;
     const int r_begin = blockIdx.y * rows_per_cta, r_end = min(nPix, r_begin + rows_per_cta);
     for (int rb = r_begin; rb < r_end; rb += kWarps) {
         __syncthreads();
         // stage kWarps rows: x-case row r = phantom[r + nPix*c]; y-case (transposed and
-        // reversed, :67) row r = phantom[(nPix-1-c) + nPix*r]
-        for (int i = threadIdx.x; i < kWarps * nPix; i += kThreads) {
+        // reversed, :67) row r = phantom[(nPix-1-c) + nPix*r]; val[nPix] = 0
+        for (int i = threadIdx.x; i < kWarps * (nPix + 1); i += kThreads) {
             int w, c;
             if (vi.axis) { w = i % kWarps; c = i / kWarps; }
-            else { w = i / nPix; c = i % nPix; }
+            else { w = i / (nPix + 1); c = i % (nPix + 1); }
             int r = rb + w;
             float v = 0.f;
-            if (r < r_end)
+            if (r < r_end && c < nPix)
                 v = vi.axis ? __ldg(phantom + r + (size_t)nPix * c)
                             : __ldg(phantom + (nPix - 1 - c) + (size_t)nPix * r);
-            tile[w * nPix + c] = v;
+            tile[w * (nPix + 1) + c] = v;
         }
         __syncthreads();
         const int r = rb + warp;
         if (r >= r_end) continue;
-        warp_prefix(val, nPix, S, lane);
-        __syncwarp();
-        double r0, delta;
-        row_affine(vi, r, nPix, G.pSize, &r0, &delta);
+        double r0d, deltad;
+        row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
+        const float r0 = (float)r0d, rdelta = (float)(1.0 / deltad), adelta = (float)std::fabs(deltad);
         for (int n = lane; n < nDet; n += 32) {
-            double P0 = row_integral(dm[n], r0, delta, S, val, nPix);
-            double P1 = row_integral(dm[n + 1], r0, delta, S, val, nPix);
-            acc[n] += (float)fabs(P1 - P0);  // :101
+            const float q0 = (dm[n] - r0) * rdelta, q1 = (dm[n + 1] - r0) * rdelta;
+            acc[n] += fabsf(row_span(val, nPix, q0, q1)) * adelta;  // |diff(Pdk)|, :101
         }
         __syncwarp();
     }
@@ -227,62 +191,78 @@ __global__ void __launch_bounds__(kThreads)
     for (int n = threadIdx.x; n < nDet; n += kThreads) {
         float s = 0.f;
         for (int w = 0; w < kWarps; w++) s += accw[w * nDet + n];
-        atomicAdd(sino + p + (size_t)G.na * n, (float)(s * L[(size_t)p * nDet + n]));  // :104
+        atomicAdd(sino + p + (size_t)G.na * n, s * L[(size_t)p * nDet + n]);  // :104
     }
 }
 
 // ------------------------------------------------------------------ backward
+// F(u) over the detector: integral of the bin densities up to u (knots K ascending).
+__device__ __forceinline__ int knot_search(const float *K, int nDet, float u) {
+    int lo = 0, hi = nDet;  // K[lo] <= u < K[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (K[mid] <= u) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 __global__ void __launch_bounds__(kThreads)
-    bdd_back_kernel(BddArgs G, const ViewInfo *info, const double *kn, const double *kv,
+    bdd_back_kernel(BddArgs G, const ViewInfo *info, const float *kn, const float *kb, const float *kinv,
                     float *image, int views_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet;
-    double *K = reinterpret_cast<double *>(smraw);    // nDet+1
-    double *V = K + (nDet + 1);                       // nDet+1
-    double *Pall = V + (nDet + 1);                    // kWarps x (nPix+1)
-    float *accX = reinterpret_cast<float *>(Pall + kWarps * (nPix + 1));  // kWarps x nPix
+    float *K = reinterpret_cast<float *>(smraw);  // nDet+1
+    float *B = K + (nDet + 1);                     // nDet
+    float *KI = B + nDet;                          // nDet
+    float *accX = KI + nDet;                       // kWarps x nPix
     float *accY = accX + kWarps * nPix;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * kWarps + warp;
     for (int i = threadIdx.x; i < 2 * kWarps * nPix; i += kThreads) accX[i] = 0.f;
-    double *P = Pall + warp * (nPix + 1);
     float *ax = accX + warp * nPix, *ay = accY + warp * nPix;
     const int v_begin = blockIdx.y * views_per_cta, v_end = min(G.na, v_begin + views_per_cta);
+    const int per = (nPix + 31) / 32;  // contiguous pixels per lane
     for (int p = v_begin; p < v_end; p++) {
         __syncthreads();
-        for (int k = threadIdx.x; k <= nDet; k += kThreads) {
-            K[k] = kn[(size_t)p * (nDet + 1) + k];
-            V[k] = kv[(size_t)p * (nDet + 1) + k];
+        for (int k = threadIdx.x; k <= nDet; k += kThreads) K[k] = kn[(size_t)p * (nDet + 1) + k];
+        for (int j = threadIdx.x; j < nDet; j += kThreads) {
+            B[j] = kb[(size_t)p * nDet + j];
+            KI[j] = kinv[(size_t)p * nDet + j];
         }
         __syncthreads();
         if (r >= nPix) continue;
         const ViewInfo vi = info[p];
-        double r0, delta;
-        row_affine(vi, r, nPix, G.pSize, &r0, &delta);
-        for (int c = lane; c <= nPix; c += 32) {  // Pdk = interp(detm -> Ppj)(rowm), :198-203
-            double u = r0 + c * delta, val;
-            if (!(u > K[0])) val = V[0];
-            else if (u >= K[nDet]) val = V[nDet];
-            else {
-                int lo = 0, hi = nDet;  // K[lo] <= u < K[hi]
-                while (hi - lo > 1) {
-                    int mid = (lo + hi) >> 1;
-                    if (K[mid] <= u) lo = mid; else hi = mid;
-                }
-                double t = (u - K[lo]) / (K[hi] - K[lo]);
-                val = V[lo] + t * (V[hi] - V[lo]);
-            }
-            P[c] = val;
+        double r0d, deltad;
+        row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
+        const float r0 = (float)r0d, delta = (float)deltad;
+        const float kfirst = K[0], klast = K[nDet];
+        // lane owns pixels [c_a, c_b); walk the knots forward from the first boundary
+        const int c_a = lane * per, c_b = min(nPix, c_a + per);
+        if (c_a >= c_b) continue;
+        float u0 = fmaf((float)c_a, delta, r0);
+        int j0 = knot_search(K, nDet, fminf(fmaxf(u0, kfirst), klast));
+        for (int c = c_a; c < c_b; c++) {
+            const float u1 = fmaf((float)(c + 1), delta, r0);
+            // integral of the detector density over [u0, u1] (clamped to the knots)
+            const float a = fminf(fmaxf(fminf(u0, u1), kfirst), klast);
+            const float b = fminf(fmaxf(fmaxf(u0, u1), kfirst), klast);
+            int ja = j0;
+            while (ja > 0 && K[ja] > a) ja--;
+            while (ja < nDet - 1 && K[ja + 1] <= a) ja++;
+            int jb = ja;
+            while (jb < nDet - 1 && K[jb + 1] <= b) jb++;
+            float sum = -(a - K[ja]) * KI[ja] * B[ja];
+            for (int j = ja; j < jb; j++) sum += B[j];
+            sum += (b - K[jb]) * KI[jb] * B[jb];
+            const float tmp = fabsf(sum);  // :205
+            if (vi.axis) ax[c] += tmp;       // :210
+            else ay[c] += tmp;               // :212
+            if (p == 0) ax[c] += tmp;        // aliasing of :139-140
+            u0 = u1;
+            j0 = jb;
         }
-        __syncwarp();
-        for (int c = lane; c < nPix; c += 32) {
-            float tmp = (float)fabs(P[c + 1] - P[c]);  // :205
-            if (vi.axis) ax[c] += tmp;                 // :210
-            else ay[c] += tmp;                         // :212
-            if (p == 0) ax[c] += tmp;                  // aliasing of :139-140
-        }
-        __syncwarp();
     }
+    __syncwarp();
     if (r >= nPix) return;
     for (int c = lane; c < nPix; c += 32) {
         if (ax[c] != 0.f) atomicAdd(image + r + (size_t)nPix * c, ax[c]);
@@ -293,22 +273,20 @@ __global__ void __launch_bounds__(kThreads)
 size_t info_bytes(int na) { return ((size_t)na * sizeof(ViewInfo) + 255) & ~(size_t)255; }
 
 size_t project_smem(const BddArgs &G) {
-    return sizeof(double) * ((size_t)(G.nDet + 1) + (size_t)kWarps * (G.nPix + 1)) +
-           sizeof(float) * ((size_t)kWarps * G.nPix + (size_t)kWarps * G.nDet);
+    return sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * (G.nPix + 1) + (size_t)kWarps * G.nDet);
 }
 size_t back_smem(const BddArgs &G) {
-    return sizeof(double) * (2 * (size_t)(G.nDet + 1) + (size_t)kWarps * (G.nPix + 1)) +
-           sizeof(float) * (2 * (size_t)kWarps * G.nPix);
+    return sizeof(float) * ((size_t)(G.nDet + 1) + 2 * (size_t)G.nDet + 2 * (size_t)kWarps * G.nPix);
 }
 
 }  // namespace
 
 size_t bdd_project_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + sizeof(double) * ((size_t)G.na * (G.nDet + 1) + (size_t)G.na * G.nDet);
+    return info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + (size_t)G.na * G.nDet);
 }
 
 size_t bdd_back_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + sizeof(double) * (3 * (size_t)G.na * (G.nDet + 1));
+    return info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + 2 * (size_t)G.na * G.nDet);
 }
 
 int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
@@ -319,10 +297,10 @@ int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void
         return SGB_ERR_ARG;
     }
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
-    double *detm = reinterpret_cast<double *>(static_cast<char *>(scratch) + info_bytes(G.na));
-    double *L = detm + (size_t)G.na * (G.nDet + 1);
+    float *detm = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
+    float *L = detm + (size_t)G.na * (G.nDet + 1);
     SGB_CUDA(cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)G.na * G.nDet, st));
-    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, detm, L, nullptr, nullptr, nullptr);
+    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, detm, L, nullptr, nullptr, nullptr, nullptr);
     SGB_TRY(after_launch("bdd_setup_kernel"));
     int rsplit = std::max(1, std::min((G.nPix + kWarps - 1) / kWarps, (2 * 152 + G.na - 1) / G.na));
     int rows = (G.nPix + rsplit - 1) / rsplit;
@@ -340,18 +318,18 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
         return SGB_ERR_ARG;
     }
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
-    double *detm = reinterpret_cast<double *>(static_cast<char *>(scratch) + info_bytes(G.na));
-    double *kn = detm + (size_t)G.na * (G.nDet + 1);
-    double *kv = kn + (size_t)G.na * (G.nDet + 1);
+    float *kn = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
+    float *kb = kn + (size_t)G.na * (G.nDet + 1);
+    float *kinv = kb + (size_t)G.na * G.nDet;
     SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
-    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, detm, nullptr, sino, kn, kv);
+    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, nullptr, nullptr, sino, kn, kb, kinv);
     SGB_TRY(after_launch("bdd_setup_kernel"));
     int gx = (G.nPix + kWarps - 1) / kWarps;
     int vsplit = std::max(1, std::min(G.na, (2 * 152 + gx - 1) / gx));
     int vpc = (G.na + vsplit - 1) / vsplit;
     vsplit = (G.na + vpc - 1) / vpc;
     SGB_CUDA(cudaFuncSetAttribute(bdd_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, kn, kv, image, vpc);
+    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, kn, kb, kinv, image, vpc);
     return after_launch("bdd_back_kernel");
 }
 

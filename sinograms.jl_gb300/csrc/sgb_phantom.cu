@@ -119,32 +119,50 @@ __global__ void ellipsoid_proj_kernel(int is_arc, int ns, int nt, int na, const 
 }
 
 // Pixel image of ellipses (ImageGeom order, x fastest): mean over sub x sub samples per
-// pixel of the indicator sums; ell rows (cx, cy, rx, ry, angle, density).
+// pixel of the indicator sums; ell rows (cx, cy, rx, ry, angle, density).  FP32 (the
+// per-ellipse terms are prepared in FP64 per block).
+constexpr int kMaxImgEll = 64;
 __global__ void ellipse_image_kernel(int nx, int ny, double dx, double dy, double ox, double oy,
                                      const double *__restrict__ ell, int nell, int sub, float *img) {
+    __shared__ float E[kMaxImgEll][7];  // cx, cy, cos, sin, 1/rx, 1/ry, density
+    for (int e = threadIdx.x; e < nell; e += blockDim.x) {
+        const double *Q = ell + 6 * e;
+        double sa, ca;
+        sincos(Q[4], &sa, &ca);
+        E[e][0] = (float)Q[0];
+        E[e][1] = (float)Q[1];
+        E[e][2] = (float)ca;
+        E[e][3] = (float)sa;
+        E[e][4] = (float)(1.0 / Q[2]);
+        E[e][5] = (float)(1.0 / Q[3]);
+        E[e][6] = (float)Q[5];
+    }
+    __syncthreads();
     const int ix = blockIdx.x * blockDim.x + threadIdx.x, iy = blockIdx.y;
     if (ix >= nx) return;
-    const double xc = dx * (ix - ((nx - 1) / 2.0 + ox)), yc = dy * (iy - ((ny - 1) / 2.0 + oy));
-    double acc = 0;
+    const float xc = (float)(dx * (ix - ((nx - 1) / 2.0 + ox))), yc = (float)(dy * (iy - ((ny - 1) / 2.0 + oy)));
+    float acc = 0.f;
     for (int a = 0; a < sub; a++)
         for (int b = 0; b < sub; b++) {
-            const double x = xc + dx * ((a + 0.5) / sub - 0.5), y = yc + dy * ((b + 0.5) / sub - 0.5);
+            const float x = xc + (float)dx * ((a + 0.5f) / sub - 0.5f), y = yc + (float)dy * ((b + 0.5f) / sub - 0.5f);
             for (int e = 0; e < nell; e++) {
-                const double *E = ell + 6 * e;
-                double sa, ca;
-                sincos(E[4], &sa, &ca);
-                const double u = ((x - E[0]) * ca + (y - E[1]) * sa) / E[2];
-                const double v = (-(x - E[0]) * sa + (y - E[1]) * ca) / E[3];
-                if (u * u + v * v <= 1.0) acc += E[5];
+                const float px = x - E[e][0], py = y - E[e][1];
+                const float u = (px * E[e][2] + py * E[e][3]) * E[e][4];
+                const float v = (-px * E[e][3] + py * E[e][2]) * E[e][5];
+                if (u * u + v * v <= 1.f) acc += E[e][6];
             }
         }
-    img[ix + (long long)nx * iy] = (float)(acc / (sub * sub));
+    img[ix + (long long)nx * iy] = acc / (sub * sub);
 }
 
 }  // namespace
 
 int launch_ellipse_image(int nx, int ny, double dx, double dy, double ox, double oy, const double *ell_dev,
                          int nell, int sub, float *img, cudaStream_t st) {
+    if (nell > kMaxImgEll) {
+        set_error("ellipse_image: at most %d ellipses per call", kMaxImgEll);
+        return SGB_ERR_ARG;
+    }
     if (nx <= 0 || ny <= 0) return SGB_OK;
     ellipse_image_kernel<<<dim3(floor_div_up(nx, 128), ny), 128, 0, st>>>(nx, ny, dx, dy, ox, oy, ell_dev, nell, sub,
                                                                            img);
