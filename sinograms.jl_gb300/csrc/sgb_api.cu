@@ -78,7 +78,11 @@ struct sgb_plan {
     std::vector<double> Hk;
     int ndet = 0, nrow = 1, na = 0;  // ns|nb, nt|1, na
     // device tables
-    DevBuf gext, wA, wB, trig, betas, xds, yds, zds, mask;
+    FilterOperator filt;  // ramp filter as a split-BF16 GEMM operator (tensor cores)
+    int *filt_err = nullptr;  // device word for the filter's error flags (flags[3], or a batch's)
+    DevBuf split;             // split differenced rows between the filter's two kernels
+    DevBuf *split_shared = nullptr;  // a batch's common scratch (its scans filter one after another)
+    DevBuf wA, wB, trig, betas, xds, yds, zds, mask;
     const uint8_t *mask_dev = nullptr;
     long long sAj = 0, sAa = 0, sBj = 0, sBt = 0;
     bool hasA = false, hasB = false;
@@ -105,6 +109,21 @@ struct sgb_plan {
 
 namespace {
 
+int filter_status(int e) {
+    if (!e) return SGB_OK;
+    set_error("filter: tensor-core kernel reported error flags 0x%x (wait timeout)", e);
+    return SGB_ERR_TIMEOUT;
+}
+
+// finish() plus, for synchronous calls, the filter's error word
+int plan_done(sgb_plan *P, int flags, cudaStream_t st) {
+    SGB_TRY(finish(flags, st));
+    if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
+    int e = 0;
+    SGB_CUDA(cudaMemcpy(&e, P->filt_err, sizeof(int), cudaMemcpyDeviceToHost));
+    return filter_status(e);
+}
+
 int plan_common(sgb_plan *P, int kind, int ndet, double d, double dsd, const sgb_filter_opts *opt,
                 int nrow, int na, const double *ar, cudaStream_t st) {
     sgb_filter_opts o{};
@@ -125,9 +144,11 @@ int plan_common(sgb_plan *P, int kind, int ndet, double d, double dsd, const sgb
     }
     std::vector<double> g;
     spatial_kernel(P->Hk, g);
-    std::vector<float> gx;
-    build_gext(g, ndet, gx);
-    SGB_TRY(upload_raw(gx.data(), gx.size() * sizeof(float), P->gext, st));
+    // three BF16 pieces (FP32-class rows); two when the filtered rows are stored in BF16
+    SGB_TRY(P->filt.build(g, ndet, (ndet + 7) / 8 * 8, P->storage == SGB_STORE_BF16 ? 2 : 3, st));
+    SGB_TRY(P->flags.reserve(4 * sizeof(int)));
+    SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
+    P->filt_err = P->flags.as<int>() + 3;
     double w;
     SGB_TRY(angle_weight(ar, na, &w));
     P->scale = (float)w;
@@ -240,8 +261,6 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     P->pitch = (g.ns + 7) / 8 * 8;
     SGB_TRY(P->filt_buf.reserve((size_t)P->pitch * g.nt * g.na * elem));
     SGB_CUDA(cudaMemsetAsync(P->filt_buf.p, 0, (size_t)P->pitch * g.nt * g.na * elem, st));
-    SGB_TRY(P->flags.reserve(4 * sizeof(int)));
-    SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
     FdkTmaArgs &A = P->targs;
     A.trig = P->trig.as<float2>();
     A.ns = g.ns;
@@ -439,8 +458,9 @@ static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *o
     A.sBj = P->sBj;
     A.sBt = P->sBt;
     A.scale = P->scale;
-    A.gext = P->gext.as<float>();
-    return launch_filter_rows(A, out, P->storage == SGB_STORE_BF16, st);
+    A.err = P->filt_err;
+    return launch_filter_rows(A, P->filt, P->split_shared ? *P->split_shared : P->split, out,
+                              P->storage == SGB_STORE_BF16, st);
 }
 
 int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *stream) {
@@ -472,13 +492,13 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
             SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
         SGB_TRY(finish(flags, st));
         if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
-        int err = 0;
-        SGB_CUDA(cudaMemcpy(&err, P->targs.err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (err) {
-            set_error("fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", err);
-            return (err & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
+        int err[2] = {0, 0};
+        SGB_CUDA(cudaMemcpy(err, P->flags.as<int>() + 2, sizeof err, cudaMemcpyDeviceToHost));
+        if (err[0]) {
+            set_error("fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", err[0]);
+            return (err[0] & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
         }
-        return SGB_OK;
+        return filter_status(err[1]);
     }
     FdkArgs A{};
     A.proj = P->filt_buf.p;
@@ -508,7 +528,7 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     P->mark(2, st);
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
-    return finish(flags, st);
+    return plan_done(P, flags, st);
 }
 
 int sgb_fbp(sgb_plan *P, const float *sino, float *image, int nslices, int flags, void *stream) {
@@ -553,7 +573,7 @@ int sgb_fbp(sgb_plan *P, const float *sino, float *image, int nslices, int flags
     P->mark(2, st);
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(image, img_dev, npix * sizeof(float), cudaMemcpyDeviceToHost, st));
-    return finish(flags, st);
+    return plan_done(P, flags, st);
 }
 
 // Stages of fbp(plan, sino): the plan's weights + ramp filter, and its back-projector.
@@ -573,7 +593,7 @@ int sgb_fbp_filter_rows(sgb_plan *P, const float *sino, float *filtered, int nsl
     SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.na * nslices, out_dev, st));
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(filtered, out_dev, n * sizeof(float), cudaMemcpyDeviceToHost, st));
-    return finish(flags, st);
+    return plan_done(P, flags, st);
 }
 
 int sgb_fbp_backproject(sgb_plan *P, const float *filtered, float *image, int nslices, int flags, void *stream) {
@@ -624,10 +644,9 @@ int sgb_fbp_sino_filter(const float *in, int nb, long long nrows, const double *
     cudaStream_t st = as_stream(stream);
     std::vector<double> hk(Hk, Hk + npad), g;
     spatial_kernel(hk, g);
-    std::vector<float> gx;
-    build_gext(g, nb, gx);
-    DevBuf dg, din, dout;
-    SGB_TRY(upload_raw(gx.data(), gx.size() * sizeof(float), dg, st));
+    FilterOperator F;
+    SGB_TRY(F.build(g, nb, nb + extra, 3, st));
+    DevBuf din, dout, split;
     const void *in_dev;
     SGB_TRY(stage_in(in, sizeof(float) * nb * (size_t)nrows, flags, din, &in_dev, st));
     float *out_dev = out;
@@ -644,10 +663,10 @@ int sgb_fbp_sino_filter(const float *in, int nb, long long nrows, const double *
     A.nt = 1;
     A.na = 1;
     A.scale = 1.f;
-    A.gext = dg.as<float>();
-    SGB_TRY(launch_filter_rows(A, out_dev, 0, st));
+    SGB_TRY(launch_filter_rows(A, F, split, out_dev, 0, st));
     if (!(flags & SGB_DEVICE_PTRS)) SGB_CUDA(cudaMemcpyAsync(out, out_dev, out_bytes, cudaMemcpyDeviceToHost, st));
-    return finish(flags, st);
+    SGB_TRY(finish(flags, st));
+    return F.check(st);  // the operator and staging buffers are freed on return
 }
 
 int sgb_cbct_back(float *image, const float *proj, int ns, int nt, int na, const double *betas,
@@ -823,7 +842,7 @@ int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const dou
 
 struct sgb_batch {
     std::vector<sgb_plan *> plans;
-    DevBuf scans, work, counter, flags;
+    DevBuf scans, work, counter, flags, split;
     std::vector<FdkBatchArgs> classes;  // one persistent launch per box-width class
     std::vector<int> class_ctas;
     FdkBatchArgs args{};                // totals for sgb_batch_fdk_info
@@ -867,6 +886,13 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     }
     SGB_TRY(B->flags.reserve(4 * sizeof(int)));
     SGB_CUDA(cudaMemsetAsync(B->flags.p, 0, 4 * sizeof(int), st));
+    size_t split_bytes = 0;
+    for (sgb_plan *P : B->plans) {
+        P->filt_err = B->flags.as<int>() + 1;  // flags[1]: every scan's filter
+        P->split_shared = &B->split;
+        split_bytes = std::max(split_bytes, filter_scratch_bytes(P->filt, (long long)P->cg.nt * P->cg.na));
+    }
+    SGB_TRY(B->split.reserve(split_bytes));  // no allocation may happen during capture
     SGB_TRY(B->counter.reserve(4 * sizeof(int)));
     // per-scan tensor maps (each with its own box width) and device argument table
     std::vector<FdkTmaArgs> scans(n);
@@ -1010,13 +1036,14 @@ int sgb_batch_fdk_run(sgb_batch *B, int flags, void *stream) {
     g_launches.fetch_add((long long)(B->plans.size() + B->classes.size()), std::memory_order_relaxed);
     if (flags & SGB_ASYNC) return SGB_OK;
     SGB_CUDA(cudaStreamSynchronize(st));
-    int err = 0;
-    SGB_CUDA(cudaMemcpy(&err, B->args.err, sizeof(int), cudaMemcpyDeviceToHost));
-    if (err) {
-        set_error("batch_fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", err);
-        return (err & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
+    int err[2] = {0, 0};
+    SGB_CUDA(cudaMemcpy(err, B->flags.p, sizeof err, cudaMemcpyDeviceToHost));
+    if (err[0]) {
+        set_error("batch_fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)",
+                  err[0]);
+        return (err[0] & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
     }
-    return SGB_OK;
+    return filter_status(err[1]);
 }
 
 int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n) {

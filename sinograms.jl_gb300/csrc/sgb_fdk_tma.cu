@@ -215,19 +215,6 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
-
 template <typename TP, bool ARC, int ZU, int BW, int VPS>
 int launch_v(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
     dim3 grid(floor_div_up(A.nx, kTX), floor_div_up(A.ny, kTY), floor_div_up(A.nz, ZU));
@@ -253,6 +240,20 @@ int launch_t(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
 }
 
 }  // namespace
+
+// cuTensorMapEncodeTiled from the driver (no libcuda link dependency).
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
 
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage) {
     return 128 + (size_t)nstage * vps * A.box_bytes + (sizeof(int2) + sizeof(float2)) * nstage * vps +

@@ -1,5 +1,8 @@
 // sgb_kernels.cuh -- launch interfaces of the CUDA kernels (internal).
 #pragma once
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <vector>
 
 #include "sgb_common.cuh"
@@ -10,7 +13,7 @@ namespace sgb {
 struct FilterArgs {
     const float *in;     // (ns, nrows)
     int ns;              // samples per row (nb)
-    int nout;            // output row length (ns + extra)
+    int nout;            // output row length (ns + extra, or the pitch); columns >= ns are zero
     long long nrows;     // nt * na * nslices
     int nt, na;          // row r -> t = r % nt, a = (r / nt) % na
     const float *wA;     // A[j*sAj + a*sAa] or null
@@ -18,11 +21,33 @@ struct FilterArgs {
     const float *wB;     // B[j*sBj + t*sBt] or null
     long long sBj, sBt;
     float scale;         // scalar weight (dbeta)
-    const float *gext;   // (2ns-1) Toeplitz kernel
+    // set by launch_filter_rows
+    void *out;
+    int kpad, nblk;      // K padded to the stage width; 256-column output blocks
+    int ovec;            // 16-byte vector stores of outputs
+    int *err;            // device error flags (wait timeouts)
 };
-int launch_filter_rows(const FilterArgs &A, void *out, int out_bf16, cudaStream_t st);
-void build_gext(const std::vector<double> &g, int ns, std::vector<float> &gext);
-size_t filter_smem_bytes(int ns);
+
+// The filter as a GEMM operator: the suffix-summed Toeplitz matrix H (rows = outputs,
+// K = input samples) split into np BF16 pieces in device memory, with its TMA map.
+struct FilterOperator {
+    int ns = 0, np = 0, kpad = 0, nblk = 0;
+    DevBuf buf, err;
+    CUtensorMap map;
+    ~FilterOperator();
+    // g: real(ifft(Hk)) (length npad); outputs up to nout_max columns per row
+    int build(const std::vector<double> &g, int ns, int nout_max, int np, cudaStream_t st);
+    // reads back (and reports) the kernel's error flags; synchronises st
+    int check(cudaStream_t st);
+};
+// Weighted, differenced, split rows go through `scratch` (grown to filter_scratch_bytes;
+// pre-size it before stream capture).
+size_t filter_scratch_bytes(const FilterOperator &F, long long nrows);
+int launch_filter_rows(const FilterArgs &A, const FilterOperator &F, DevBuf &scratch, void *out, int out_bf16,
+                       cudaStream_t st);
+
+// cuTensorMapEncodeTiled from the driver entry-point table (null when unavailable)
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn();
 
 // ---------------------------------------------------- view geometry table
 // per used view v (view index a = v * ia_skip): (sin, cos) in FP32 from FP64 angles.

@@ -84,6 +84,24 @@ def test_sino_filter_random(cuda, nb, npad):
     close(S.fbp_sino_filter(x, Hk), O.sino_filter(x, Hk), maxrel=2e-4)
 
 
+def test_sino_filter_many_tiles_smooth_rows(cuda):
+    """Persistent tensor-core filter over many 128-row tiles (both accumulators of every
+    CTA in use), three 256-sample output blocks, and smooth rows on which the ramp filter
+    cancels ~100x -- the case the split-BF16 GEMM on first differences is built for."""
+    nb, npad, nrows = 520, 1024, 40000
+    rng = np.random.default_rng(7)
+    s = np.arange(nb)[None, :]
+    c = rng.uniform(100, 420, (nrows, 1))
+    w = rng.uniform(40, 90, (nrows, 1))
+    x = np.sqrt(np.clip(w * w - (s - c) ** 2, 0, None)) * rng.uniform(0.5, 2.0, (nrows, 1))
+    x = x.astype(np.float32)
+    Hk = O.fbp_filter(dict(kind="flat", nb=nb, d=1.0), npad=npad)
+    ref = O.sino_filter_fft(x.astype(np.float64), Hk)
+    out = S.fbp_sino_filter(x, Hk, extra=5)
+    assert out.shape == (nrows, nb + 5) and np.all(out[:, nb:] == 0)
+    close(out[:, :nb], ref, rmse=1e-6, maxrel=1e-5)
+
+
 def test_bdd_fixtures(cuda):
     f, g = fix("bdd"), C.BDD
     geo = S.BddGeo(g["DSD"], g["DS0"], g["pSize"], g["dSize"], g["nPix"], g["nDet"], g["angle"])
