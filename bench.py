@@ -182,7 +182,9 @@ def run_ours(args):
                               filter_ms=float(np.mean(fms)), back_ms=float(np.mean(bms)), gpu_launches=launches,
                               clocks=clocks, plan=plan)
         outs[storage] = img
-    head = "bf16"
+    # headline: the FP32 form (the BF16 storage form is reported beside it with its
+    # accuracy; its ~1.8e-4 rel RMSE vs FP64 misses the 1e-4 bound on this workload)
+    head = "f32"
     # e2e through the public API with pinned host buffers (H2D of the projections and
     # D2H of the volume inside the timed region, every step)
     plan = forms[head]["plan"]
@@ -213,13 +215,13 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic: 30 seeded random ellipsoids, analytic cone-beam "
         "projections generated on the GPU",
         "config": {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5,
-                   "storage": "bf16 filtered projections, fp32 arithmetic", "updates_per_step": upd,
+                   "storage": "fp32 filtered projections, fp32 arithmetic", "updates_per_step": upd,
                    "l2": "inputs larger than L2 (566 MB projections per step)", "parallelism": f"replicas x{ws}"},
         "forms": {k: {"value": v["value"], "ms_per_step": v["ms_per_step"], "filter_ms": v["filter_ms"],
                       "back_ms": v["back_ms"]} for k, v in forms.items()},
         "e2e": {"value": ws * upd * args.steps / e2e_s, "unit": UNIT,
                 "h2d_bytes_per_step": proj.numel() * 4, "d2h_bytes_per_step": nvox * 4},
-        "roofline": {"bound": "hbm", "kernel": "fdk_back_kernel", "achieved": achieved, "peak": hbm,
+        "roofline": {"bound": "hbm", "kernel": "fdk_tma_kernel", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
                      "alg_bytes_per_launch": alg_bytes,
@@ -238,9 +240,7 @@ def run_ours(args):
         base, acc = cpu_leg({k: v.cpu().numpy() for k, v in outs.items()}, proj.cpu().numpy())
         line["cpu_baseline"] = base
         line["accuracy_vs_fp64"] = acc
-        if acc["bf16"]["rel_rmse"] > 1e-4:  # headline form must meet the accuracy bound
-            line["value"] = forms["f32"]["value"]
-            line["config"]["storage"] = "fp32 (bf16 form exceeded 1e-4 rel RMSE)"
+        line["forms"]["bf16"]["meets_1e-4"] = bool(acc["bf16"]["rel_rmse"] <= 1e-4)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -150,66 +150,13 @@ __global__ void __launch_bounds__(kThreads)
         const FdkTmaArgs &A = *S;
         const int ngroups = (A.nv + VPS - 1) / VPS;
         const int nvalid = min(VPS, A.nv - tg.y * VPS);
-        const int ns = A.ns, nt = A.nt, H = A.H;
-        for (int v = 0; v < nvalid; v++) {
-            const float2 sc = vtrig[st * VPS + v];
-            const int2 o = origin[st * VPS + v];
-            const TP *box = reinterpret_cast<const TP *>(stage_base + (size_t)(st * VPS + v) * box_bytes);
-            float bs, mag, w2;
-            if (A.is_arc) column_map<true>(A, x, y, sc.x, sc.y, &bs, &mag, &w2);
-            else column_map<false>(A, x, y, sc.x, sc.y, &bs, &mag, &w2);
-            const float fis = floorf(bs);
-            if (!(fis >= 1.f && fis < (float)ns)) continue;
-            const int c = (int)fis - 1 - o.x;
-            if (c < 0 || c > W - 2) {
-                atomicOr(B.err, 1);
-                continue;
-            }
-            const float fs = bs - fis;
-            const float magt = mag * A.inv_dtds;
-            const float bt0 = fmaf(magt, z0, A.wt), dbt = magt * A.dz;
-            const int lo = max(1, o.y + 1), hi = min(nt - 1, o.y + H - 1);
-            if (hi < lo) continue;
-            const float b_last = fmaf((float)(ZU - 1), dbt, bt0);
-            const int r0 = (int)floorf(clampf(fminf(bt0, b_last), -1e7f, 1e7f));
-            const int r1 = (int)floorf(clampf(fmaxf(bt0, b_last), -1e7f, 1e7f));
-            {
-                const int v0 = max(1, r0), v1 = min(nt - 1, r1);
-                if (v0 <= v1 && (v0 < lo || v1 > hi)) atomicOr(B.err, 1);
-            }
-            const TP *base = box + c - (o.y + 1) * W;
-            if (r0 >= lo && r1 <= hi) {
-#pragma unroll
-                for (int k = 0; k < ZU; k++) {
-                    const float bt = fmaf((float)k, dbt, bt0);
-                    const float fit = floorf(bt);
-                    const TP *p = base + (int)fit * W;
-                    const float ft = bt - fit;
-                    const float p00 = sload(p), p10 = sload(p + 1);
-                    const float p01 = sload(p + W), p11 = sload(p + W + 1);
-                    const float a0 = fmaf(fs, p10 - p00, p00);
-                    const float a1 = fmaf(fs, p11 - p01, p01);
-                    acc[k] = fmaf(w2, fmaf(ft, a1 - a0, a0), acc[k]);
-                }
-                continue;
-            }
-            const unsigned span = (unsigned)(hi - lo);
-#pragma unroll
-            for (int k = 0; k < ZU; k++) {
-                const float bt = fmaf((float)k, dbt, bt0);
-                const float fit = floorf(bt);
-                const int it = (int)fit;
-                const bool okr = (unsigned)(it - lo) <= span;
-                const TP *p = base + (okr ? it : lo) * W;
-                const float wk = okr ? w2 : 0.f;
-                const float ft = bt - fit;
-                const float p00 = sload(p), p10 = sload(p + 1);
-                const float p01 = sload(p + W), p11 = sload(p + W + 1);
-                const float a0 = fmaf(fs, p10 - p00, p00);
-                const float a1 = fmaf(fs, p11 - p01, p01);
-                acc[k] = fmaf(wk, fmaf(ft, a1 - a0, a0), acc[k]);
-            }
-        }
+        const int H = A.H;
+        if (A.is_arc)
+            stage_views<TP, true, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+                                         stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, B.err);
+        else
+            stage_views<TP, false, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+                                          stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, B.err);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + st);
         if (tg.y == ngroups - 1 && ix < A.nx && iy < A.ny) {  // tile complete: write the voxels

@@ -127,8 +127,6 @@ __global__ void __launch_bounds__(kThreads)
     float acc[ZU];
 #pragma unroll
     for (int k = 0; k < ZU; k++) acc[k] = 0.f;
-    const int ns = A.ns, nt = A.nt;
-
     for (int g = 0; g < ngroups; g++) {
         const int st = g % NSTAGE, round = g / NSTAGE;
         const bool ok = mbar_wait(full + st, round & 1);
@@ -137,68 +135,8 @@ __global__ void __launch_bounds__(kThreads)
             break;
         }
         const int nvalid = min(VPS, A.nv - g * VPS);
-        for (int v = 0; v < nvalid; v++) {
-            const float2 sc = vtrig[st * VPS + v];
-            const int2 o = origin[st * VPS + v];
-            const TP *box = reinterpret_cast<const TP *>(stage_base + (size_t)(st * VPS + v) * box_bytes);
-            float bs, mag, w2;
-            column_map<ARC>(A, x, y, sc.x, sc.y, &bs, &mag, &w2);
-            const float fis = floorf(bs);
-            if (!(fis >= 1.f && fis < (float)ns)) continue;  // cbct-back.jl:197 (s part)
-            const int c = (int)fis - 1 - o.x;                  // box column of sample is-1
-            if (c < 0 || c > W - 2) {
-                atomicOr(A.err, 1);
-                continue;
-            }
-            const float fs = bs - fis;
-            const float magt = mag * A.inv_dtds;
-            const float bt0 = fmaf(magt, z0, A.wt), dbt = magt * A.dz;
-            // rows usable: reference range [1, nt-1] intersected with the box
-            const int lo = max(1, o.y + 1), hi = min(nt - 1, o.y + H - 1);
-            if (hi < lo) continue;
-            // rows of the first and last voxel bound the thread's rows (bt is monotone in k)
-            const float b_last = fmaf((float)(ZU - 1), dbt, bt0);
-            const int r0 = (int)floorf(clampf(fminf(bt0, b_last), -1e7f, 1e7f));
-            const int r1 = (int)floorf(clampf(fmaxf(bt0, b_last), -1e7f, 1e7f));
-            {
-                // a reference-valid row outside the box would be an undersized box
-                const int v0 = max(1, r0), v1 = min(nt - 1, r1);
-                if (v0 <= v1 && (v0 < lo || v1 > hi)) atomicOr(A.err, 1);
-            }
-            const TP *base = box + c - (o.y + 1) * W;  // row it (1-based) -> box row it-1-t0
-            if (r0 >= lo && r1 <= hi) {
-                // every voxel of the column hits a valid, staged row: no per-voxel test
-#pragma unroll
-                for (int k = 0; k < ZU; k++) {
-                    const float bt = fmaf((float)k, dbt, bt0);
-                    const float fit = floorf(bt);
-                    const TP *p = base + (int)fit * W;
-                    const float ft = bt - fit;
-                    const float p00 = sload(p), p10 = sload(p + 1);
-                    const float p01 = sload(p + W), p11 = sload(p + W + 1);
-                    const float a0 = fmaf(fs, p10 - p00, p00);
-                    const float a1 = fmaf(fs, p11 - p01, p01);
-                    acc[k] = fmaf(w2, fmaf(ft, a1 - a0, a0), acc[k]);
-                }
-                continue;
-            }
-            const unsigned span = (unsigned)(hi - lo);
-#pragma unroll
-            for (int k = 0; k < ZU; k++) {
-                const float bt = fmaf((float)k, dbt, bt0);          // :189,192
-                const float fit = floorf(bt);
-                const int it = (int)fit;
-                const bool ok = (unsigned)(it - lo) <= span;          // :197 (t part) and in-box
-                const TP *p = base + (ok ? it : lo) * W;              // dropped taps read a safe row
-                const float wk = ok ? w2 : 0.f;
-                const float ft = bt - fit;
-                const float p00 = sload(p), p10 = sload(p + 1);
-                const float p01 = sload(p + W), p11 = sload(p + W + 1);
-                const float a0 = fmaf(fs, p10 - p00, p00);          // :205
-                const float a1 = fmaf(fs, p11 - p01, p01);          // :206
-                acc[k] = fmaf(wk, fmaf(ft, a1 - a0, a0), acc[k]);   // :208
-            }
-        }
+        stage_views<TP, ARC, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+                                    stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, A.err);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + st);
     }

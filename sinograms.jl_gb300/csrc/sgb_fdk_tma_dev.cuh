@@ -83,13 +83,162 @@ __device__ __forceinline__ void tile_coords(const FdkTmaArgs &A, int bx, int by,
     *zhi = fmaxf(za, zb);
 }
 
-template <typename TP>
-__device__ __forceinline__ float sload(const TP *p) {
-    return static_cast<float>(*p);
+
+
+// floor(v) for |v| < 2^22 without the conversion units (16 results per clock per SM):
+// the round-down add m = v + 1.5 * 2^23 leaves floor(v) in the low mantissa bits of m
+// (bits(m) = floor(v) + 0x4B400000), and m - 1.5 * 2^23 is floor(v) exactly.
+
+// Shared-memory loads by 32-bit address (the box addresses below are computed in 32-bit
+// arithmetic, wrapping, and only valid rows are dereferenced).
+__device__ __forceinline__ float lds(const float *, uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
 }
-template <>
-__device__ __forceinline__ float sload<__nv_bfloat16>(const __nv_bfloat16 *p) {
-    return __bfloat162float(*p);
+__device__ __forceinline__ float lds(const __nv_bfloat16 *, uint32_t a) {
+    unsigned short h;
+    asm volatile("ld.shared.u16 %0, [%1];" : "=h"(h) : "r"(a));
+    return __uint_as_float((uint32_t)h << 16);
+}
+
+// (a != b) ? x : y as one compare and one select, never a branch.
+__device__ __forceinline__ float sel_ne(uint32_t a, uint32_t b, float x, float y) {
+    float d;
+    asm("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %1, %2;\n\tselp.f32 %0, %3, %4, p;\n\t}"
+        : "=f"(d)
+        : "r"(a), "r"(b), "f"(x), "f"(y));
+    return d;
+}
+
+// Geometry of one (column, view) pair for cbct_back_fan_voxel (cbct-back.jl:170-210):
+// voxels z0 + k dz, k < ZU, of the column (x, y), read from the view's staged detector
+// box (W samples per row, H rows, origin o).  `mode` selects the form that applies:
+//   0  no contribution (s tap outside [1, ns) or no valid row)
+//   1  streaming: every voxel's rows are valid and staged and consecutive voxels advance
+//      at most one detector row (0 <= dbt < 1), so each voxel loads only its upper row's
+//      two taps and reuses the s-interpolated lower row of the voxel before
+//   2  fast: every voxel's rows valid and staged (four taps per voxel)
+//   3  checked: per-voxel reference edge rule (dropped taps read a safe row, weight 0)
+// All forms perform the same floating-point operations per voxel, so results do not
+// depend on the form.
+struct ColView {
+    int mode;
+    float fs, w2, bt0, dbt;
+    int lo, hi;
+    uint32_t sb;  // shared address of the box element at 1-based row 0, column of tap is-1
+};
+
+template <typename TP, bool ARC, int ZU, int W>
+__device__ __forceinline__ ColView view_setup(const FdkTmaArgs &A, float x, float y, float z0, float2 sc, int2 o,
+                                              int H, uint32_t box, int *err) {
+    ColView g;
+    g.mode = 0;
+    float bs, mag;
+    column_map<ARC>(A, x, y, sc.x, sc.y, &bs, &mag, &g.w2);
+    const float fis = floorf(bs);
+    if (!(fis >= 1.f && fis < (float)A.ns)) return g;  // cbct-back.jl:197 (s part)
+    const int c = (int)fis - 1 - o.x;                    // box column of sample is-1
+    if (c < 0 || c > W - 2) {
+        atomicOr(err, 1);
+        return g;
+    }
+    g.fs = bs - fis;
+    const float magt = mag * A.inv_dtds;
+    g.bt0 = fmaf(magt, z0, A.wt);  // :189,192
+    g.dbt = magt * A.dz;
+    // rows usable: reference range [1, nt-1] intersected with the box
+    g.lo = max(1, o.y + 1);
+    g.hi = min(A.nt - 1, o.y + H - 1);
+    if (g.hi < g.lo) return g;
+    // rows of the first and last voxel bound the column's rows (bt is monotone in k)
+    const float b_last = fmaf((float)(ZU - 1), g.dbt, g.bt0);
+    const int r0 = (int)floorf(clampf(fminf(g.bt0, b_last), -1e7f, 1e7f));
+    const int r1 = (int)floorf(clampf(fmaxf(g.bt0, b_last), -1e7f, 1e7f));
+    {
+        // a reference-valid row outside the box would be an undersized box
+        const int v0 = max(1, r0), v1 = min(A.nt - 1, r1);
+        if (v0 <= v1 && (v0 < g.lo || v1 > g.hi)) atomicOr(err, 1);
+    }
+    g.sb = box + (uint32_t)((c - (o.y + 1) * W) * (int)sizeof(TP));  // row it (1-based) -> box row it-1-t0
+    if (r0 >= g.lo && r1 <= g.hi) g.mode = (g.dbt < 0.999f && g.dbt >= 0.f) ? 1 : 2;
+    else g.mode = 3;
+    return g;
+}
+
+template <typename TP, int ZU, int W>
+__device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) {
+    constexpr uint32_t RB = W * sizeof(TP), SZ = sizeof(TP);  // bytes per box row / sample
+    const TP *tag = nullptr;
+    if (g.mode == 1) {
+        // magic_floor's bits are it + 0x4B400000: fold that offset into the base address
+        const uint32_t kb = g.sb - 0x4B400000u * RB;
+        float m = __fadd_rd(g.bt0, 12582912.0f);
+        uint32_t bits = __float_as_uint(m), a = kb + bits * RB;
+        float p0 = lds(tag, a), p1 = lds(tag, a + SZ);
+        float lo_v = fmaf(g.fs, p1 - p0, p0);  // :205
+        p0 = lds(tag, a + RB);
+        p1 = lds(tag, a + RB + SZ);
+        float hi_v = fmaf(g.fs, p1 - p0, p0);  // :206
+        acc[0] = fmaf(g.w2, fmaf(g.bt0 - (m - 12582912.0f), hi_v - lo_v, lo_v), acc[0]);  // :208
+        uint32_t prev = bits;
+#pragma unroll
+        for (int k = 1; k < ZU; k++) {
+            const float bt = fmaf((float)k, g.dbt, g.bt0);
+            m = __fadd_rd(bt, 12582912.0f);
+            bits = __float_as_uint(m);
+            a = kb + RB + bits * RB;  // upper row it+1
+            const float q0 = lds(tag, a), q1 = lds(tag, a + SZ);
+            const float nv = fmaf(g.fs, q1 - q0, q0);
+            lo_v = sel_ne(bits, prev, hi_v, lo_v);  // advanced one row: the old upper row
+            hi_v = nv;
+            prev = bits;
+            acc[k] = fmaf(g.w2, fmaf(bt - (m - 12582912.0f), hi_v - lo_v, lo_v), acc[k]);
+        }
+    } else if (g.mode == 2) {
+        const uint32_t kb = g.sb - 0x4B400000u * RB;
+#pragma unroll
+        for (int k = 0; k < ZU; k++) {
+            const float bt = fmaf((float)k, g.dbt, g.bt0);
+            const float m = __fadd_rd(bt, 12582912.0f);
+            const uint32_t a = kb + __float_as_uint(m) * RB;
+            const float ft = bt - (m - 12582912.0f);
+            const float p00 = lds(tag, a), p10 = lds(tag, a + SZ);
+            const float p01 = lds(tag, a + RB), p11 = lds(tag, a + RB + SZ);
+            const float a0 = fmaf(g.fs, p10 - p00, p00);
+            const float a1 = fmaf(g.fs, p11 - p01, p01);
+            acc[k] = fmaf(g.w2, fmaf(ft, a1 - a0, a0), acc[k]);
+        }
+    } else if (g.mode == 3) {
+        const unsigned span = (unsigned)(g.hi - g.lo);
+#pragma unroll
+        for (int k = 0; k < ZU; k++) {
+            const float bt = fmaf((float)k, g.dbt, g.bt0);          // :189,192
+            const float fit = floorf(bt);
+            const int it = (int)fit;
+            const bool ok = (unsigned)(it - g.lo) <= span;          // :197 (t part) and in-box
+            const uint32_t a = g.sb + (uint32_t)((ok ? it : g.lo) * (int)RB);  // dropped taps read a safe row
+            const float wk = ok ? g.w2 : 0.f;
+            const float ft = bt - fit;
+            const float p00 = lds(tag, a), p10 = lds(tag, a + SZ);
+            const float p01 = lds(tag, a + RB), p11 = lds(tag, a + RB + SZ);
+            const float a0 = fmaf(g.fs, p10 - p00, p00);           // :205
+            const float a1 = fmaf(g.fs, p11 - p01, p01);           // :206
+            acc[k] = fmaf(wk, fmaf(ft, a1 - a0, a0), acc[k]);       // :208
+        }
+    }
+}
+
+// Views [0, nvalid) of a stage, in order.
+template <typename TP, bool ARC, int ZU, int W>
+__device__ __forceinline__ void stage_views(const FdkTmaArgs &A, float x, float y, float z0, const float2 *vtrig,
+                                            const int2 *origin, int H, const unsigned char *boxes, int box_bytes,
+                                            int nvalid, float (&acc)[ZU], int *err) {
+    const uint32_t b0 = smem_u32(boxes);
+    for (int v = 0; v < nvalid; v++)
+        view_scalar<TP, ZU, W>(
+            view_setup<TP, ARC, ZU, W>(A, x, y, z0, vtrig[v], origin[v], H, b0 + (uint32_t)(v * box_bytes), err),
+            acc);
 }
 
 }  // namespace fdkdev
