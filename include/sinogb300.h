@@ -77,7 +77,11 @@ typedef struct {
     double dod;           /* fan only */
 } sgb_sino_geom;
 
-/* CtFanArc / CtFanFlat fields, src/geom/type3.jl:145-184 (circular source) */
+/* Source trajectories, src/geom/ct-source.jl: CtSourceCircle, CtSourceHelix(pitch, source_z0) */
+#define SGB_SRC_CIRCLE 0
+#define SGB_SRC_HELIX 1
+
+/* CtFanArc / CtFanFlat fields, src/geom/type3.jl:145-184 */
 typedef struct {
     int kind; /* SGB_ARC or SGB_FLAT */
     int ns, nt;
@@ -86,6 +90,9 @@ typedef struct {
     int na;
     double orbit, orbit_start;
     double source_offset, dsd, dod;
+    int src;          /* SGB_SRC_CIRCLE (0, the default) or SGB_SRC_HELIX */
+    float pitch;      /* CtSourceHelix.pitch (Float32, fraction of zFOV per turn) */
+    double source_z0; /* CtSourceHelix.source_z0 */
 } sgb_ct_geom;
 
 /* ImageGeom (ImageGeoms.jl 0.11): centres x_i = delta*(i - (n+1)/2 - offset). */
@@ -106,6 +113,9 @@ typedef struct {
     int decon1;                /* default 1 */
     const double *filter;      /* optional user Hk of length npad (overrides the above) */
     int storage;               /* SGB_STORE_F32 or SGB_STORE_BF16 */
+    int source_z;              /* FDK with a helical source: 0 ignores the source z as cbct_back does
+                                  (cbct-back.jl:188-189); 1 back-projects t' = mag * (z - source_zs[view]),
+                                  the line the reference leaves commented at cbct-back.jl:188 */
 } sgb_filter_opts;
 
 typedef struct sgb_plan sgb_plan;
@@ -122,6 +132,8 @@ SGB_API long long sgb_launch_count(void);
 SGB_API int sgb_fbp_ramp(int kind, int N, double ds, double dsd, double *h);
 /* fbp_window, src/fbp/window.jl:298-312 (fftshift'ed, Float32-valued) */
 SGB_API int sgb_fbp_window(int shape, double cutoff, int N, const double *vect, double *win);
+/* _source_zs(rg), src/geom/ct-geom.jl:125-140: source z of each view (zeros for a circle) */
+SGB_API int sgb_source_zs(const sgb_ct_geom *rg, double *zs);
 /* fbp_filter, src/fbp/filter.jl:32-57 */
 SGB_API int sgb_fbp_filter(int kind, int npad, double ds, double dsd, int shape, double cutoff,
                    const double *vect, int decon1, double *Hk);

@@ -278,10 +278,13 @@ void orc_fbp_sino_weight(const double *gam, int nb, double dso, double source_of
 /* cbct_back_fan! + cbct_back_fan_voxel, src/fbp3/cbct-back.jl:95-213.
  * proj (ns, nt, na); image (nx, ny, nz); mask may be NULL (all true).
  * betas has na entries; views ia = 1:ia_skip:na are used (:121-125). */
-int orc_cbct_back(real_t *image, const real_t *proj, int ns, int nt, int na, const double *betas,
-                  double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
-                  int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
-                  int nz, const uint8_t *mask, int ia_skip) {
+/* cbct_back with a per-view source z (zs_ds[ia] = source_zs[ia] / ds, or NULL for the
+ * reference's z_src = 0): t' = mag * (z_ds - source_zs[ia]), the form left commented at
+ * cbct-back.jl:188.  With NULL this is exactly cbct_back_fan_voxel. */
+int orc_cbct_back_zs(real_t *image, const real_t *proj, int ns, int nt, int na, const double *betas,
+                     double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
+                     int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
+                     int nz, const uint8_t *mask, int ia_skip, const double *zs_ds) {
     if (ia_skip < 1) return ORC_ERR_ARG;
     float ws = (float)((ns + 1) / 2.0 + offset_s); /* :119 Toffset(...) */
     float wt = (float)((nt + 1) / 2.0 + offset_t); /* :120 */
@@ -317,7 +320,7 @@ int orc_cbct_back(real_t *image, const real_t *proj, int ns, int nt, int na, con
                 sprime_ds = mag * x_beta;
                 w2 = mag * mag;
             }
-            real_t tprime_ds = mag * (z_ds - 0);                   /* :189 */
+            real_t tprime_ds = mag * (z_ds - (zs_ds ? (real_t)zs_ds[vidx[v]] : 0)); /* :188-189 */
             real_t bs = sprime_ds + (real_t)ws;                   /* :191 */
             real_t bt = tprime_ds / dt_ds + (real_t)wt;           /* :192 */
             long is = (long)floor(bs), it = (long)floor(bt);       /* :194-195 */
@@ -334,6 +337,14 @@ int orc_cbct_back(real_t *image, const real_t *proj, int ns, int nt, int na, con
     }
     free(sb); free(cb); free(vidx);
     return ORC_OK;
+}
+
+int orc_cbct_back(real_t *image, const real_t *proj, int ns, int nt, int na, const double *betas,
+                  double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
+                  int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
+                  int nz, const uint8_t *mask, int ia_skip) {
+    return orc_cbct_back_zs(image, proj, ns, nt, na, betas, dsd, dso, ds, dt, offset_s, offset_t, is_arc, xc, yc,
+                            zc, nx, ny, nz, mask, ia_skip, NULL);
 }
 
 /* ------------------------------------------------------------- back-par.jl */

@@ -247,8 +247,22 @@ def sino_filter(x: np.ndarray, Hk: np.ndarray, extra: int = 0, bits: int = 64) -
 
 # ------------------------------------------------------------------ back-projectors
 
-def cbct_back(proj: np.ndarray, rg, ig, ia_skip: int = 1, bits: int = 64, betas=None) -> np.ndarray:
-    """cbct_back, cbct-back.jl:25-45 -> image numpy (nz, ny, nx)."""
+def source_zs(rg) -> np.ndarray:
+    """_source_zs(rg), ct-geom.jl:118-140: zeros for a circle; for a helix (rg["pitch"],
+    rg["source_z0"]) z_i = i * pitch * zfov / (na * 360/orbit) + source_z0, zfov = dso/dsd*nt*dt."""
+    na = int(_f(rg, "na"))
+    if _f(rg, "src", "circle") != "helix":
+        return np.zeros(na)
+    zfov = dso(rg) / float(_f(rg, "dsd")) * int(_f(rg, "nt")) * float(_f(rg, "dt"))
+    pitch = float(np.float32(_f(rg, "pitch", 0.0)))  # CtSourceHelix.pitch::Float32
+    dz = 0.0 if na == 1 else pitch * zfov / (na * (360 / float(_f(rg, "orbit"))))
+    return np.arange(na) * dz + float(_f(rg, "source_z0", 0.0))
+
+
+def cbct_back(proj: np.ndarray, rg, ig, ia_skip: int = 1, bits: int = 64, betas=None, zs=None) -> np.ndarray:
+    """cbct_back, cbct-back.jl:25-45 -> image numpy (nz, ny, nx).  ``zs`` (per view, length
+    units) applies the helical shift t' = mag (z - zs[ia]) the reference leaves commented at
+    cbct-back.jl:188; None is the reference's z_src = 0."""
     dt_ = np.float64 if bits == 64 else np.float32
     proj = np.ascontiguousarray(proj, dtype=dt_)
     na, nt, ns = proj.shape
@@ -257,20 +271,24 @@ def cbct_back(proj: np.ndarray, rg, ig, ia_skip: int = 1, bits: int = 64, betas=
     img = np.zeros((nz, ny, nx), dtype=dt_)
     b = np.ascontiguousarray(ar(rg) if betas is None else betas, dtype=np.float64)
     m = _mask(ig)
-    _check(lib(bits).orc_cbct_back(
+    zsd = None if zs is None else np.ascontiguousarray(np.asarray(zs, np.float64) / float(_f(rg, "ds")))
+    _check(lib(bits).orc_cbct_back_zs(
         _ptr(img), _ptr(proj), ns, nt, na, _ptr(b), _c_double(float(_f(rg, "dsd"))), _c_double(dso(rg)),
         _c_double(float(_f(rg, "ds"))), _c_double(float(_f(rg, "dt"))),
         _c_float(float(_f(rg, "offset_s", 0.0))), _c_float(float(_f(rg, "offset_t", 0.0))),
-        int(_f(rg, "kind") == "arc"), _ptr(xc), _ptr(yc), _ptr(zc), nx, ny, nz, _ptr(m), ia_skip), "cbct_back")
+        int(_f(rg, "kind") == "arc"), _ptr(xc), _ptr(yc), _ptr(zc), nx, ny, nz, _ptr(m), ia_skip, _ptr(zsd)),
+        "cbct_back")
     return img
 
 
-def fdk(rg, ig, proj: np.ndarray, shape="none", cutoff=1.0, npad=None, decon1=True, bits=64) -> np.ndarray:
-    """fdk, fdk.jl:65-81 with plan_fbp, plan3.jl:60-72."""
+def fdk(rg, ig, proj: np.ndarray, shape="none", cutoff=1.0, npad=None, decon1=True, bits=64,
+        source_z=False) -> np.ndarray:
+    """fdk, fdk.jl:65-81 with plan_fbp, plan3.jl:60-72 (source_z: the helical shift of
+    cbct_back's commented line 188 with _source_zs(rg))."""
     Hk = fbp_filter(rg, npad, shape, cutoff, decon1=decon1)
     p = np.asarray(proj, dtype=np.float64) * fdk_weights(rg)
     p = sino_filter(p, Hk, bits=bits)
-    return cbct_back(p, rg, ig, bits=bits)
+    return cbct_back(p, rg, ig, bits=bits, zs=source_zs(rg) if source_z else None)
 
 
 def fbp_back(g, ig, sino: np.ndarray, ia_skip: int = 1, bits: int = 64) -> np.ndarray:

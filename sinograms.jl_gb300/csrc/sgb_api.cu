@@ -83,6 +83,7 @@ struct sgb_plan {
     DevBuf split;             // split differenced rows between the filter's two kernels
     DevBuf *split_shared = nullptr;  // a batch's common scratch (its scans filter one after another)
     DevBuf wA, wB, trig, betas, xds, yds, zds, mask;
+    DevBuf zsrc;  // helical shift: source z / ds per view (FP32), empty for z_src = 0
     const uint8_t *mask_dev = nullptr;
     long long sAj = 0, sAa = 0, sBj = 0, sBt = 0;
     bool hasA = false, hasB = false;
@@ -263,6 +264,7 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     SGB_CUDA(cudaMemsetAsync(P->filt_buf.p, 0, (size_t)P->pitch * g.nt * g.na * elem, st));
     FdkTmaArgs &A = P->targs;
     A.trig = P->trig.as<float2>();
+    A.zsrc = P->zsrc.p ? P->zsrc.as<float>() : nullptr;
     A.ns = g.ns;
     A.nt = g.nt;
     A.na = g.na;
@@ -314,6 +316,7 @@ static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const
     SGB_REQUIRE(rg && ig && plan, "plan_fbp: null argument");
     SGB_REQUIRE(rg->kind == SGB_ARC || rg->kind == SGB_FLAT, "plan_fbp: CtGeom must be CtFanArc or CtFanFlat");
     SGB_REQUIRE(rg->ns > 1 && rg->nt > 1 && rg->na > 1, "plan_fbp: ns, nt, na must exceed 1");
+    SGB_REQUIRE(rg->src == SGB_SRC_CIRCLE || rg->src == SGB_SRC_HELIX, "plan_fbp: unknown CtSource %d", rg->src);
     cudaStream_t st = 0;
     sgb_plan *P = new sgb_plan();
     P->ct = true;
@@ -337,6 +340,12 @@ static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const
         P->hasB = true;
         P->sBj = 1;
         P->sBt = rg->ns;
+    }
+    if (s == SGB_OK && opt && opt->source_z && rg->src == SGB_SRC_HELIX) {
+        // t' = mag * (z - source_zs[ia]) (cbct-back.jl:188, commented in the reference)
+        std::vector<double> zs(rg->na);
+        s = sgb_source_zs(rg, zs.data());
+        if (s == SGB_OK) s = upload_f32(zs.data(), zs.size(), 1.0 / rg->ds, P->zsrc, st);
     }
     if (s == SGB_OK) s = plan_fdk_back(P, ig, st, tune);
     if (s != SGB_OK) {
@@ -505,6 +514,7 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     A.image = img_dev;
     A.mask = P->mask_dev;
     A.trig = P->trig.as<float2>();
+    A.zsrc = P->zsrc.p ? P->zsrc.as<float>() : nullptr;
     A.xds = P->xds.as<float>();
     A.yds = P->yds.as<float>();
     A.zds = P->zds.as<float>();

@@ -32,6 +32,7 @@ constexpr int kVChunk = 1024;     // views staged in shared memory per pass
 template <typename TP, bool ARC, int kZ>
 __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
     __shared__ float2 trig_s[kVChunk];
+    __shared__ float zs_s[kVChunk];  // source z / ds per view (0 for a circular orbit)
     const int ix = blockIdx.x * kBX + threadIdx.x;
     const int iy = blockIdx.y * kBY + threadIdx.y;
     const int iz0 = blockIdx.z * kZ;
@@ -55,11 +56,15 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
     for (int v0 = 0; v0 < A.nv; v0 += kVChunk) {
         const int nvc = min(kVChunk, A.nv - v0);
         __syncthreads();
-        for (int i = tid; i < nvc; i += kBX * kBY) trig_s[i] = A.trig[v0 + i];
+        for (int i = tid; i < nvc; i += kBX * kBY) {
+            trig_s[i] = A.trig[v0 + i];
+            zs_s[i] = A.zsrc ? A.zsrc[v0 + i] : 0.f;
+        }
         __syncthreads();
         if (!active) continue;
         for (int vi = 0; vi < nvc; vi++) {
             const float2 sc = trig_s[vi];
+            const float zs = zs_s[vi];
             const float sb = sc.x, cb = sc.y;
             const float xb = fmaf(x, cb, y * sb);                    // cbct-back.jl:174
             const float yb = A.dso_ds - fmaf(-x, sb, y * cb);        // :175
@@ -81,7 +86,7 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
             const TP *base = proj + (long long)(v0 + vi) * A.ia_skip * view_stride + ((int)fis - 1);
 #pragma unroll
             for (int k = 0; k < kZ; k++) {
-                const float bt = fmaf(magt, z[k], A.wt);             // :189,192
+                const float bt = fmaf(magt, z[k] - zs, A.wt);        // :188-192
                 const float fit = floorf(bt);
                 if (fit >= 1.f && fit < fnt) {                       // :197 (t part)
                     const float ft = bt - fit;

@@ -28,7 +28,8 @@ __global__ void __launch_bounds__(kThreads)
     unsigned char *stage_base = sm;
     int2 *origin = reinterpret_cast<int2 *>(sm + (size_t)NSTAGE * VPS * box_bytes);
     float2 *vtrig = reinterpret_cast<float2 *>(origin + NSTAGE * VPS);
-    int2 *tag = reinterpret_cast<int2 *>(vtrig + NSTAGE * VPS);  // [NSTAGE]: (item, group)
+    float *vzs = reinterpret_cast<float *>(vtrig + NSTAGE * VPS);  // [NSTAGE][VPS] source z / ds
+    int2 *tag = reinterpret_cast<int2 *>(vzs + NSTAGE * VPS);       // [NSTAGE]: (item, group)
     uint64_t *full = reinterpret_cast<uint64_t *>(tag + NSTAGE);
     uint64_t *empty = full + NSTAGE;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -80,15 +81,20 @@ __global__ void __launch_bounds__(kThreads)
                     const int v = g * VPS + lane;
                     int2 o = make_int2(0, 0);
                     float2 sc = make_float2(0.f, 1.f);
+                    float zs = 0.f;
                     if (v < A.nv) {
                         sc = A.trig[v];
+                        if (A.zsrc) zs = A.zsrc[v];
                         int s0, t0, w, h;
-                        if (A.is_arc) tile_box<true>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo, zhi, &s0, &t0, &w, &h);
-                        else tile_box<false>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo, zhi, &s0, &t0, &w, &h);
+                        if (A.is_arc)
+                            tile_box<true>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo - zs, zhi - zs, &s0, &t0, &w, &h);
+                        else
+                            tile_box<false>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo - zs, zhi - zs, &s0, &t0, &w, &h);
                         o = make_int2(s0, t0);
                     }
                     origin[st * VPS + lane] = o;
                     vtrig[st * VPS + lane] = sc;
+                    vzs[st * VPS + lane] = zs;
                 }
                 if (lane == 0) tag[st] = make_int2(item, g);
                 __syncwarp();
@@ -152,10 +158,10 @@ __global__ void __launch_bounds__(kThreads)
         const int nvalid = min(VPS, A.nv - tg.y * VPS);
         const int H = A.H;
         if (A.is_arc)
-            stage_views<TP, true, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+            stage_views<TP, true, ZU, W>(A, x, y, z0, vtrig + st * VPS, vzs + st * VPS, origin + st * VPS, H,
                                          stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, B.err);
         else
-            stage_views<TP, false, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+            stage_views<TP, false, ZU, W>(A, x, y, z0, vtrig + st * VPS, vzs + st * VPS, origin + st * VPS, H,
                                           stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, B.err);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + st);
@@ -201,7 +207,7 @@ int batch_occupancy(const FdkBatchArgs &B) {
 }  // namespace
 
 size_t fdk_batch_smem(const FdkBatchArgs &B) {
-    return 128 + (size_t)kNStage * B.vps * B.box_bytes + (sizeof(int2) + sizeof(float2)) * kNStage * B.vps +
+    return 128 + (size_t)kNStage * B.vps * B.box_bytes + (sizeof(int2) + sizeof(float2) + sizeof(float)) * kNStage * B.vps +
            sizeof(int2) * kNStage + 2 * sizeof(uint64_t) * kNStage;
 }
 

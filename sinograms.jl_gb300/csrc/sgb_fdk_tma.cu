@@ -40,8 +40,9 @@ __global__ void box_extent_kernel(FdkTmaArgs A, int ntx, int nty, int ntz, int *
     float xlo, xhi, ylo, yhi, zlo, zhi;
     tile_coords(A, bx, by, bz, &xlo, &xhi, &ylo, &yhi, &zlo, &zhi, ZU);
     const float2 sc = A.trig[v];
+    const float zs = A.zsrc ? A.zsrc[v] : 0.f;
     int s0, t0, w, h;
-    tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo, zhi, &s0, &t0, &w, &h);
+    tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo - zs, zhi - zs, &s0, &t0, &w, &h);
     atomicMax(ext + 0, w);
     atomicMax(ext + 1, h);
 }
@@ -58,7 +59,8 @@ __global__ void __launch_bounds__(kThreads)
     unsigned char *stage_base = sm;
     int2 *origin = reinterpret_cast<int2 *>(sm + (size_t)NSTAGE * VPS * box_bytes);  // [NSTAGE][VPS]
     float2 *vtrig = reinterpret_cast<float2 *>(origin + NSTAGE * VPS);               // [NSTAGE][VPS]
-    uint64_t *full = reinterpret_cast<uint64_t *>(vtrig + NSTAGE * VPS);
+    float *vzs = reinterpret_cast<float *>(vtrig + NSTAGE * VPS);                    // [NSTAGE][VPS]
+    uint64_t *full = reinterpret_cast<uint64_t *>(vzs + NSTAGE * VPS);
     uint64_t *empty = full + NSTAGE;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -91,14 +93,17 @@ __global__ void __launch_bounds__(kThreads)
                 const int v = g * VPS + lane;
                 int2 o = make_int2(0, 0);
                 float2 sc = make_float2(0.f, 1.f);
+                float zs = 0.f;
                 if (v < A.nv) {
                     sc = A.trig[v];
+                    if (A.zsrc) zs = A.zsrc[v];
                     int s0, t0, w, h;
-                    tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo, zhi, &s0, &t0, &w, &h);
+                    tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo - zs, zhi - zs, &s0, &t0, &w, &h);
                     o = make_int2(s0, t0);
                 }
                 origin[st * VPS + lane] = o;
                 vtrig[st * VPS + lane] = sc;
+                vzs[st * VPS + lane] = zs;
             }
             __syncwarp();
             if (lane == 0) {
@@ -135,7 +140,7 @@ __global__ void __launch_bounds__(kThreads)
             break;
         }
         const int nvalid = min(VPS, A.nv - g * VPS);
-        stage_views<TP, ARC, ZU, W>(A, x, y, z0, vtrig + st * VPS, origin + st * VPS, H,
+        stage_views<TP, ARC, ZU, W>(A, x, y, z0, vtrig + st * VPS, vzs + st * VPS, origin + st * VPS, H,
                                     stage_base + (size_t)st * VPS * box_bytes, box_bytes, nvalid, acc, A.err);
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + st);
@@ -194,7 +199,7 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage) {
-    return 128 + (size_t)nstage * vps * A.box_bytes + (sizeof(int2) + sizeof(float2)) * nstage * vps +
+    return 128 + (size_t)nstage * vps * A.box_bytes + (sizeof(int2) + sizeof(float2) + sizeof(float)) * nstage * vps +
            2 * sizeof(uint64_t) * nstage;
 }
 

@@ -8,6 +8,7 @@ namespace sgb {
 
 struct FdkTmaArgs {
     const float2 *trig;     // nv used views: (sin, cos)
+    const float *zsrc;      // nv used views: source z / ds (helical shift), or null (z_src = 0)
     float *image;           // (nx, ny, nz)
     const uint8_t *mask;    // (nx, ny, nz) or null
     int *err;               // device error flags: 1 box too small, 2 wait timeout, 4 drain timeout

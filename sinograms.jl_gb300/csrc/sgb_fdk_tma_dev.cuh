@@ -229,16 +229,16 @@ __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) 
     }
 }
 
-// Views [0, nvalid) of a stage, in order.
+// Views [0, nvalid) of a stage, in order; vzs holds each view's source z / ds.
 template <typename TP, bool ARC, int ZU, int W>
 __device__ __forceinline__ void stage_views(const FdkTmaArgs &A, float x, float y, float z0, const float2 *vtrig,
-                                            const int2 *origin, int H, const unsigned char *boxes, int box_bytes,
-                                            int nvalid, float (&acc)[ZU], int *err) {
+                                            const float *vzs, const int2 *origin, int H, const unsigned char *boxes,
+                                            int box_bytes, int nvalid, float (&acc)[ZU], int *err) {
     const uint32_t b0 = smem_u32(boxes);
-    for (int v = 0; v < nvalid; v++)
-        view_scalar<TP, ZU, W>(
-            view_setup<TP, ARC, ZU, W>(A, x, y, z0, vtrig[v], origin[v], H, b0 + (uint32_t)(v * box_bytes), err),
-            acc);
+    for (int v = 0; v < nvalid; v++)  // z relative to the view's source z (0 for a circular orbit)
+        view_scalar<TP, ZU, W>(view_setup<TP, ARC, ZU, W>(A, x, y, z0 - vzs[v], vtrig[v], origin[v], H,
+                                                          b0 + (uint32_t)(v * box_bytes), err),
+                               acc);
 }
 
 }  // namespace fdkdev

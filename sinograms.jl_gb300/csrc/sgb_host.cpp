@@ -307,6 +307,22 @@ int sgb_parker_weight_ct(const sgb_ct_geom *rg, float *w, int *n0, int *n2) {
     return SGB_OK;
 }
 
+// _source_dz_per_view / _source_zs, src/geom/ct-geom.jl:118-140: zfov = dso/dsd*nt*dt
+// (:120), dz = pitch * zfov / (na * 360/orbit) (0 when na == 1), z_i = i*dz + source_z0.
+int sgb_source_zs(const sgb_ct_geom *rg, double *zs) {
+    SGB_REQUIRE(rg && zs, "source_zs: null argument");
+    SGB_REQUIRE(rg->src == SGB_SRC_CIRCLE || rg->src == SGB_SRC_HELIX, "unknown CtSource %d", rg->src);
+    if (rg->src == SGB_SRC_CIRCLE) {
+        for (int i = 0; i < rg->na; i++) zs[i] = 0.0;
+        return SGB_OK;
+    }
+    const double zfov = (rg->dsd - rg->dod) / rg->dsd * rg->nt * rg->dt;
+    const double na_per_360 = rg->na * (360.0 / rg->orbit);
+    const double dz = rg->na == 1 ? 0.0 : (double)rg->pitch * zfov / na_per_360;
+    for (int i = 0; i < rg->na; i++) zs[i] = i * dz + rg->source_z0;
+    return SGB_OK;
+}
+
 int sgb_fdk_weight_cyl(const sgb_ct_geom *rg, double *w) {
     SGB_REQUIRE(rg && w, "fdk_weight_cyl: null pointer");
     std::vector<double> s = det_axis(rg->ns, rg->ds, rg->offset_s);

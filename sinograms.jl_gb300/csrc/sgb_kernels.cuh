@@ -60,6 +60,7 @@ struct FdkArgs {
     const uint8_t *mask;   // (nx, ny, nz) or null
     const float2 *trig;    // nv used views
     const float *xds, *yds, *zds;  // pixel centres / ds
+    const float *zsrc;     // nv used views: source z / ds, or null
     int ns, nt, na, nx, ny, nz, nv, ia_skip;
     int pitch;             // row stride of proj in elements (>= ns)
     float ws, wt;          // (ns+1)/2 + offset_s, (nt+1)/2 + offset_t (1-based)

@@ -16,6 +16,7 @@ SGB_DEVICE_PTRS, SGB_ASYNC = 1, 2
 SGB_PAR, SGB_ARC, SGB_FLAT = 0, 1, 2
 SGB_WIN = {"none": 0, "boxcar": 1, "hamming": 2, "hann": 3, "vect": 4}
 SGB_STORE_F32, SGB_STORE_BF16 = 0, 1
+SGB_SRC_CIRCLE, SGB_SRC_HELIX = 0, 1
 
 c_int, c_ll, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
 P = c_void_p
@@ -31,7 +32,8 @@ class SinoGeomC(ctypes.Structure):
 class CtGeomC(ctypes.Structure):
     _fields_ = [("kind", c_int), ("ns", c_int), ("nt", c_int), ("ds", c_double), ("dt", c_double),
                 ("offset_s", c_float), ("offset_t", c_float), ("na", c_int), ("orbit", c_double),
-                ("orbit_start", c_double), ("source_offset", c_double), ("dsd", c_double), ("dod", c_double)]
+                ("orbit_start", c_double), ("source_offset", c_double), ("dsd", c_double), ("dod", c_double),
+                ("src", c_int), ("pitch", c_float), ("source_z0", c_double)]
 
 
 class ImageGeomC(ctypes.Structure):
@@ -41,7 +43,7 @@ class ImageGeomC(ctypes.Structure):
 
 class FilterOptsC(ctypes.Structure):
     _fields_ = [("window_shape", c_int), ("cutoff", c_double), ("window_vect", P), ("npad", c_int),
-                ("decon1", c_int), ("filter", P), ("storage", c_int)]
+                ("decon1", c_int), ("filter", P), ("storage", c_int), ("source_z", c_int)]
 
 
 # (name, restype, argtypes)
@@ -56,6 +58,7 @@ _SIGS = {
     "sgb_parker_weight_sino": (c_int, [P, P, P, P]),
     "sgb_parker_weight_ct": (c_int, [P, P, P, P]),
     "sgb_fdk_weight_cyl": (c_int, [P, P]),
+    "sgb_source_zs": (c_int, [P, P]),
     "sgb_fbp_sino_weight": (c_int, [P, P]),
     "sgb_fbp_sino_filter": (c_int, [P, c_int, c_ll, P, c_int, c_int, P, c_int, P]),
     "sgb_cbct_back": (c_int, [P, P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, c_float,

@@ -13,6 +13,7 @@ image (nx, ny[, nz]) is ``([nz,] ny, nx)``.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from dataclasses import dataclass, field, replace
 
@@ -98,6 +99,22 @@ class SinoFanFlat(_SinoFan):
 
 
 @dataclass(frozen=True)
+class CtSourceCircle:
+    """Circular source trajectory (src/geom/ct-source.jl:22-26)."""
+
+
+@dataclass(frozen=True)
+class CtSourceHelix:
+    """Helical source with constant pitch (src/geom/ct-source.jl:29-56): ``pitch`` is a
+    Float32 fraction of the z field of view per turn, ``source_z0`` the first view's z."""
+    pitch: float = 0.0
+    source_z0: float = 0.0
+
+    def __post_init__(self):
+        object.__setattr__(self, "pitch", _f32(self.pitch))
+
+
+@dataclass(frozen=True)
 class _CtFan:
     ns: int = 128
     nt: int = 64
@@ -111,6 +128,7 @@ class _CtFan:
     source_offset: float = 0.0
     dsd: float | None = None
     dod: float | None = None
+    src: object = CtSourceCircle()
 
     def __post_init__(self):
         object.__setattr__(self, "offset_s", _f32(self.offset_s))
@@ -226,12 +244,34 @@ def downsample(rg, down: int):
     return replace(rg, nb=2 * max(rg.nb // (2 * down), 1), d=rg.d * down, na=max(rg.na // down, 1))
 
 
+def _zfov(rg) -> float:
+    """_zfov(rg::CtFan), ct-geom.jl:120."""
+    return _dso(rg) / rg.dsd * rg.nt * rg.dt
+
+
+def _source_dz_per_view(rg) -> float:
+    """_source_dz_per_view(rg), ct-geom.jl:123-131."""
+    if not isinstance(rg.src, CtSourceHelix) or rg.na == 1:
+        return 0.0
+    return rg.src.pitch * _zfov(rg) / (rg.na * (360 / rg.orbit))
+
+
+def _source_zs(rg) -> np.ndarray:
+    """_source_zs(rg), ct-geom.jl:134-140 (computed by the library's host code)."""
+    zs = np.zeros(rg.na)
+    _lib.check(_lib.lib().sgb_source_zs(ctypes.byref(c_struct(rg)), zs.ctypes.data), "source_zs")
+    return zs
+
+
 def c_struct(rg):
     """The C ABI struct (sgb_sino_geom / sgb_ct_geom) for a geometry."""
     kind = {"par": _lib.SGB_PAR, "arc": _lib.SGB_ARC, "flat": _lib.SGB_FLAT}[rg.kind]
     if is_ct(rg):
+        helix = isinstance(rg.src, CtSourceHelix)
         return _lib.CtGeomC(kind, rg.ns, rg.nt, rg.ds, rg.dt, rg.offset_s, rg.offset_t, rg.na, rg.orbit,
-                            rg.orbit_start, rg.source_offset, rg.dsd, rg.dod)
+                            rg.orbit_start, rg.source_offset, rg.dsd, rg.dod,
+                            _lib.SGB_SRC_HELIX if helix else _lib.SGB_SRC_CIRCLE,
+                            rg.src.pitch if helix else 0.0, rg.src.source_z0 if helix else 0.0)
     return _lib.SinoGeomC(kind, rg.nb, rg.d, rg.offset, rg.na, rg.orbit, rg.orbit_start,
                           getattr(rg, "source_offset", 0.0), getattr(rg, "dsd", 0.0) or 0.0,
                           getattr(rg, "dod", 0.0) or 0.0)

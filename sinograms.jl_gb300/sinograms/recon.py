@@ -24,7 +24,7 @@ def _status(st: int, what: str):
 class _Plan:
     """Owner of a library plan handle (sgb_plan)."""
 
-    def __init__(self, rg, ig: ImageGeom, window: Window, npad, decon1, filter, storage):
+    def __init__(self, rg, ig: ImageGeom, window: Window, npad, decon1, filter, storage, source_z=False):
         self.rg, self.ig = rg, ig
         self.window = window
         self.storage = storage
@@ -46,6 +46,7 @@ class _Plan:
             opts.filter = f.ctypes.data
             opts.npad = len(f)
         opts.storage = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16}[storage]
+        opts.source_z = int(bool(source_z))
         self._h = ctypes.c_void_p()
         g, cig = c_struct(rg), ig.c_struct()
         fn = "sgb_plan_fbp_ct" if is_ct(rg) else "sgb_plan_fbp_sino"
@@ -100,13 +101,18 @@ class FDKplan(_Plan):
 
 
 def plan_fbp(rg, ig: ImageGeom, window: Window = Window(), npad: int | None = None, decon1: bool = True,
-             filter=None, storage: str = "f32"):
+             filter=None, storage: str = "f32", source_z: bool = False):
     """plan_fbp(rg, ig; window, npad, decon1, filter), plan2.jl:106-138 / plan3.jl:60-72.
 
-    ``storage`` ("f32" or "bf16") selects how FDK keeps the filtered projections on the
-    GPU (an addition of this implementation; 2D plans always use "f32")."""
+    Additions of this implementation: ``storage`` ("f32" or "bf16") selects how FDK keeps
+    the filtered projections on the GPU (2D plans always use "f32"); ``source_z=True``
+    back-projects a CtSourceHelix scan with t' = mag * (z - source_zs[view]) -- the shift
+    the reference leaves commented at cbct-back.jl:188 -- instead of ignoring the source z
+    as the reference's cbct_back does."""
     if is_ct(rg):
-        return FDKplan(rg, ig, window, npad, decon1, filter, storage)
+        return FDKplan(rg, ig, window, npad, decon1, filter, storage, source_z)
+    if source_z:
+        raise SinogramsArgumentError("source_z applies to CT (FDK) plans")
     if storage != "f32":
         raise SinogramsArgumentError("2D plans keep filtered sinograms in f32")
     return FBPNormalPlan(rg, ig, window, npad, decon1, filter, storage)
@@ -216,7 +222,7 @@ class FDKBatch:
     batched entry point; it reconstructs one scan per `fdk` call (fdk.jl:65-81)."""
 
     def __init__(self, rgs, igs, window: Window = Window(), npad: int | None = None, decon1: bool = True,
-                 storage: str = "f32"):
+                 storage: str = "f32", source_z: bool = False):
         n = len(rgs)
         if n != len(igs) or n == 0:
             raise SinogramsArgumentError("need one ImageGeom per scan")
@@ -231,6 +237,8 @@ class FDKBatch:
         opts.npad = int(npad or 0)
         opts.decon1 = int(decon1)
         opts.storage = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16}[storage]
+        opts.source_z = int(bool(source_z))
+        opts.source_z = int(bool(source_z))
         self._h = ctypes.c_void_p()
         _status(_lib.lib().sgb_batch_fdk_create(n, G, I, ctypes.byref(opts), ctypes.byref(self._h)),
                 "batch_fdk_create")

@@ -47,6 +47,10 @@ ARC_SHORT = dict(rg=short(_ARC, 48), ig=PAR["ig"], window="none")
 FLAT = dict(rg=dict(_ARC, kind="flat"), ig=PAR["ig"], window="hamming")
 BDD = dict(DSD=300.0, DS0=180.0, pSize=2.0, dSize=2.3, nPix=32, nDet=40, angle=np.arange(24) * (2 * math.pi / 24))
 FILTER_WRAP = dict(nb=24, npad=32, extra=3, rows=5)
+# helical source (CtSourceHelix, ct-source.jl:29-56): half a zFOV of travel per turn,
+# centred so the source z sweeps the image's z extent
+HELIX = dict(rg=ct("flat", src="helix", pitch=0.5, source_z0=-5.4, offset_s=0.25),
+             ig=dict(dims=(16, 14, 12), deltas=(1.0, 1.1, 0.9), offsets=(0.5, -0.25, 0.3)))
 
 
 def cyl_mask(ig, r):
@@ -62,6 +66,8 @@ def to_geom(g):
     g = dict(g)
     kind = g.pop("kind")
     if "ns" in g:
+        if g.pop("src", "circle") == "helix":
+            g["src"] = S.CtSourceHelix(pitch=g.pop("pitch"), source_z0=g.pop("source_z0"))
         return (S.CtFanArc if kind == "arc" else S.CtFanFlat)(**g)
     if kind == "par":
         return S.SinoPar(**g)

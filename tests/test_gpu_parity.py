@@ -55,6 +55,31 @@ def test_fdk_ragged_sizes(cuda, kind, storage):
     close(S.fdk(plan, proj), ref, *((RTOL_RMSE, MAX_REL) if storage == "f32" else (2e-3, 2e-2)))
 
 
+def test_fdk_helix_default_ignores_source_z(cuda):
+    """A CtSourceHelix scan reconstructs exactly like its circular twin unless asked
+    (the reference's cbct_back ignores source z, cbct-back.jl:188-189)."""
+    c = C.HELIX
+    circ = {k: v for k, v in c["rg"].items() if k not in ("src", "pitch", "source_z0")}
+    proj = O.ellipsoid_proj(circ, C.ELL3).astype(np.float32)
+    a = S.fdk(S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"])), proj)
+    b = S.fdk(S.plan_fbp(C.to_geom(circ), C.to_image(c["ig"])), proj)
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_fdk_helix_source_z(cuda, storage):
+    """source_z=True: t' = mag * (z - source_zs[view]) in the TMA back-projector (box
+    pre-pass and producer use the shifted z) against the oracle."""
+    c = C.HELIX
+    proj = O.ellipsoid_proj(c["rg"], C.ELL3).astype(np.float32)
+    ref = O.fdk(c["rg"], c["ig"], proj, source_z=True)
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), storage=storage, source_z=True)
+    assert plan.info()["tma"]
+    out = S.fdk(plan, proj)
+    close(out, ref, *((RTOL_RMSE, MAX_REL) if storage == "f32" else (2e-3, 2e-2)))
+    assert O.rel_rmse(out, O.fdk(c["rg"], c["ig"], proj)) > 1e-2  # the shift matters here
+
+
 def test_fdk_arc_short_fixture_mask_window(cuda):
     f, c = fix("fdk_arc_short"), C.FDK_ARC_SHORT
     mask = C.cyl_mask(c["ig"], c["mask_r"])

@@ -109,3 +109,31 @@ def test_cases_match_reference_short_constructor():
     g = C.short(dict(kind="arc", nb=128, d=1.0, offset=0.0, dsd=512.0), 128)
     assert g["na"] == S.SinoFanArc.short().na
     assert g["orbit"] == pytest.approx(S.SinoFanArc.short().orbit)
+
+
+@pytest.mark.parametrize("pitch,na,orbit", [(0.5, 24, 360.0), (1.25, 37, 270.0), (0.0, 10, 360.0), (0.7, 1, 360.0)])
+def test_source_zs_helix(pitch, na, orbit):
+    """_source_zs / _source_dz_per_view (ct-geom.jl:118-140) from the library's host code,
+    the Python mirror and the oracle restatement."""
+    g = C.ct("arc", src="helix", pitch=pitch, source_z0=-3.0, na=na, orbit=orbit)
+    rg = C.to_geom(g)
+    zs = S._source_zs(rg)
+    ref = O.source_zs(g)
+    np.testing.assert_allclose(zs, ref, rtol=0, atol=1e-12)
+    zfov = (g["dsd"] - g["dod"]) / g["dsd"] * g["nt"] * g["dt"]
+    dz = 0.0 if na == 1 else float(np.float32(pitch)) * zfov / (na * 360 / orbit)
+    assert S._source_dz_per_view(rg) == pytest.approx(dz, abs=1e-15)
+    np.testing.assert_allclose(zs, np.arange(na) * dz - 3.0, rtol=0, atol=1e-12)
+    assert np.all(S._source_zs(C.to_geom(C.ct("flat", na=na))) == 0)
+
+
+def test_oracle_helix_shift_sign():
+    """A constant source z c equals a circular scan of the grid shifted by -c in z:
+    t' = mag * (z - c) (the commented cbct-back.jl:188)."""
+    rg, ig = C.ct("flat", na=12), dict(dims=(8, 7, 6), deltas=(1.0, 1.0, 0.8), offsets=(0.0, 0.0, 0.25))
+    proj = O.ellipsoid_proj(rg, C.ELL3)
+    c = 0.6
+    shifted = O.cbct_back(proj, rg, ig, zs=np.full(12, c))
+    ig2 = dict(ig, offsets=(0.0, 0.0, 0.25 + c / 0.8))
+    np.testing.assert_allclose(shifted, O.cbct_back(proj, rg, ig2), rtol=1e-12, atol=1e-12)
+    np.testing.assert_array_equal(O.cbct_back(proj, rg, ig, zs=None), O.cbct_back(proj, rg, ig))
