@@ -266,6 +266,20 @@ SGB_API int sgb_lf_train_step(sgb_lf *lf, const float *z, const float *target, l
                               float lr, double *loss, int flags, void *stream);
 SGB_API int sgb_lf_destroy(sgb_lf *lf);
 
+/* ------------------------------------------------- sys2 geometry helpers */
+/* footprint_size(st, ig), src/sys2/footprint.jl:19-36: maximum footprint of a pixel in
+ * detector samples (Float32).  Arc/flat fans return SGB_ERR_GEOM ("bad dso") when the
+ * image's radial FOV exceeds 0.99 dso. */
+SGB_API int sgb_footprint_size_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig, float *size);
+SGB_API int sgb_footprint_size_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, float *size);
+/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59: Radon transform of the
+ * Zwart-Powell box spline at radius r (pixel units) and angle phi (host, FP64). */
+SGB_API double sgb_zwart_powell(double r, double phi);
+/* out[i + nr*j] = zwart_powell(r[i], phi[j]) for a grid of radii and angles (the
+ * reference's zwart_powell.(r, phi')), evaluated on the GPU in FP64. */
+SGB_API int sgb_zwart_powell_sino(const double *r, int nr, const double *phi, int nphi, double *out, int flags,
+                                  void *stream);
+
 /* ------------------------------------------------------------ batched FDK */
 /* No counterpart in the reference (it reconstructs one scan per fdk call,
  * src/fbp3/fdk.jl:65-81): up to 64 independent CtFanArc/CtFanFlat scans of different sizes

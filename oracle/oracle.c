@@ -659,3 +659,38 @@ void orc_ellipsoid_cone(const double *ell, int nell, int is_arc, const double *s
             }
         }
 }
+
+
+/* ---------------------------------------------------------------- sys2 */
+/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59 (always FP64, like the reference's
+ * Float64 call).  BoxSp_k is written as the sum over the 2^m signed corners of the
+ * active directions (the same central differences, expanded). */
+static double orc_zp0(double y, int n) { return y > 0 ? pow(y, n - 1) : 0.0; }
+double orc_zwart_powell(double r, double phi) {
+    const double TOL = 1e-07, s = sin(phi), c = cos(phi);
+    const double z[4] = {c, s, c + s, c - s};
+    int n = 0;
+    for (int k = 0; k < 4; k++) n += fabs(z[k]) > TOL;
+    /* BoxSp4(y) = sum over sign patterns of the active z_k of (prod sign_k) y'^(N-1)_+ / prod z_k,
+     * y' = y + sum_k sign_k z_k / 2 */
+    double acc = 0, den = 1;
+    for (int k = 0; k < 4; k++)
+        if (fabs(z[k]) > TOL) den *= z[k];
+    for (int m = 0; m < 16; m++) {
+        double y = r, sg = 1;
+        int skip = 0;
+        for (int k = 0; k < 4; k++) {
+            const int plus = (m >> k) & 1;
+            if (fabs(z[k]) > TOL) {
+                y += plus ? 0.5 * z[k] : -0.5 * z[k];
+                sg *= plus ? 1 : -1;
+            } else if (!plus) {
+                skip = 1; /* an inactive direction contributes one term, not two */
+            }
+        }
+        if (!skip) acc += sg * orc_zp0(y, n);
+    }
+    double f = 1;
+    for (int k = 2; k < n; k++) f *= k;
+    return acc / den / f;
+}

@@ -415,3 +415,32 @@ def sino_filter_fft(x: np.ndarray, Hk: np.ndarray, workers: int = 1, chunk_rows:
         F *= H
         out[r0:r0 + chunk_rows] = sfft.ifft(F, axis=-1, workers=workers).real[:, :nb]
     return out.reshape(x.shape)
+
+
+# ---------------------------------------------------------------- sys2
+def zwart_powell(r, phi):
+    """zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59 (C restatement, FP64)."""
+    f = lib(64).orc_zwart_powell
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double, ctypes.c_double]
+    return np.vectorize(lambda a, b: f(float(a), float(b)))(r, phi)
+
+
+def footprint_size(g, ig) -> float:
+    """footprint_size(st, ig), src/sys2/footprint.jl:7-36, as Float32.  fovs(ig) =
+    dims .* |deltas| (ImageGeoms 0.11)."""
+    d = ig["deltas"]
+    di = math.hypot(d[0], d[1])
+    rfov = max(ig["dims"][0] * abs(d[0]), ig["dims"][1] * abs(d[1])) / 2
+    ct = is_ct(g)
+    ratio = di / float(_f(g, "ds") if ct else _f(g, "d"))
+    kind = _f(g, "kind")
+    if kind == "par":
+        return float(np.float32(ratio))
+    if rfov > 0.99 * dso(g):
+        raise ValueError("bad dso")
+    dsd = float(_f(g, "dsd"))
+    if kind == "arc":
+        return float(np.float32(ratio * dsd / (dso(g) - rfov)))
+    smax = float(np.max(np.abs(s_axis(g))))
+    return float(np.float32(ratio * math.sqrt(dsd ** 2 + smax ** 2) / (dso(g) - rfov)))

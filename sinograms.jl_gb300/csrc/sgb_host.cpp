@@ -10,6 +10,7 @@
 
 #include "sgb_common.cuh"
 #include "sgb_host.h"
+#include "sgb_zp.cuh"
 
 namespace sgb {
 
@@ -322,6 +323,54 @@ int sgb_source_zs(const sgb_ct_geom *rg, double *zs) {
     for (int i = 0; i < rg->na; i++) zs[i] = i * dz + rg->source_z0;
     return SGB_OK;
 }
+
+// footprint_size, src/sys2/footprint.jl:7-36.  Pixel diagonal sqrt(dx^2 + dy^2) (:9);
+// radial FOV max(fovs(ig)[1:2]) / 2 with fovs = dims .* |deltas| (ImageGeoms 0.11) (:10).
+static double footprint_di(const sgb_image_geom *ig) {
+    return std::sqrt(ig->deltas[0] * ig->deltas[0] + ig->deltas[1] * ig->deltas[1]);
+}
+static double footprint_rfov(const sgb_image_geom *ig) {
+    return std::fmax(ig->dims[0] * std::fabs(ig->deltas[0]), ig->dims[1] * std::fabs(ig->deltas[1])) / 2;
+}
+
+// fan forms (:25-36): ratio * dsd / (dso - rfov) (arc), ratio * sqrt(dsd^2 + smax^2) / (dso - rfov) (flat)
+static int footprint_fan(int kind, double ratio, double dsd, double dso, double smax, const sgb_image_geom *ig,
+                         float *size) {
+    const double rfov = footprint_rfov(ig);
+    if (rfov > 0.99 * dso) {
+        set_error("bad dso");  // footprint.jl:28, :34
+        return SGB_ERR_GEOM;
+    }
+    const double num = kind == SGB_ARC ? dsd : std::sqrt(dsd * dsd + smax * smax);
+    *size = (float)(ratio * num / (dso - rfov));
+    return SGB_OK;
+}
+
+int sgb_footprint_size_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig, float *size) {
+    SGB_REQUIRE(rg && ig && size, "footprint_size: null argument");
+    SGB_REQUIRE(ig->ndim == 2, "footprint_size: SinoGeom needs a 2D ImageGeom");
+    const double ratio = footprint_di(ig) / rg->d;  // :12
+    if (rg->kind == SGB_PAR) {
+        *size = (float)ratio;  // :22
+        return SGB_OK;
+    }
+    double smax = 0;
+    for (int i = 0; i < rg->nb; i++)
+        smax = std::fmax(smax, std::fabs(rg->d * (i - ((rg->nb - 1) / 2.0 + rg->offset))));  // _s, sino-geom.jl:287
+    return footprint_fan(rg->kind, ratio, rg->dsd, rg->dsd - rg->dod, smax, ig, size);
+}
+
+int sgb_footprint_size_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, float *size) {
+    SGB_REQUIRE(rg && ig && size, "footprint_size: null argument");
+    SGB_REQUIRE(ig->ndim == 3, "footprint_size: CtGeom needs a 3D ImageGeom");
+    const double ratio = footprint_di(ig) / rg->ds;  // :13
+    double smax = 0;
+    for (int i = 0; i < rg->ns; i++)
+        smax = std::fmax(smax, std::fabs(rg->ds * (i - ((rg->ns - 1) / 2.0 + rg->offset_s))));  // _s, ct-geom.jl:148
+    return footprint_fan(rg->kind, ratio, rg->dsd, rg->dsd - rg->dod, smax, ig, size);
+}
+
+double sgb_zwart_powell(double r, double phi) { return zwart_powell_value(r, phi); }
 
 int sgb_fdk_weight_cyl(const sgb_ct_geom *rg, double *w) {
     SGB_REQUIRE(rg && w, "fdk_weight_cyl: null pointer");

@@ -59,6 +59,10 @@ _SIGS = {
     "sgb_parker_weight_ct": (c_int, [P, P, P, P]),
     "sgb_fdk_weight_cyl": (c_int, [P, P]),
     "sgb_source_zs": (c_int, [P, P]),
+    "sgb_footprint_size_sino": (c_int, [P, P, P]),
+    "sgb_footprint_size_ct": (c_int, [P, P, P]),
+    "sgb_zwart_powell": (c_double, [c_double, c_double]),
+    "sgb_zwart_powell_sino": (c_int, [P, c_int, P, c_int, P, c_int, P]),
     "sgb_fbp_sino_weight": (c_int, [P, P]),
     "sgb_fbp_sino_filter": (c_int, [P, c_int, c_ll, P, c_int, c_int, P, c_int, P]),
     "sgb_cbct_back": (c_int, [P, P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, c_float,

@@ -265,3 +265,16 @@ def test_fdk_bf16_form_error_level(cuda):
     # 720-view benchmark phantom and ~3e-4 here: the 1e-4 bound is not met by BF16
     # storage; the bound checked is the measured level.
     assert e16 < 5e-4, e16
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_zwart_powell_sino_gpu(cuda, device):
+    """zwart_powell.(r, phi') of test/sys2/zwart_powell.jl:8-10 on the GPU (FP64) against the
+    oracle restatement."""
+    r = np.linspace(-1, 1, 101) * 2
+    phi = np.linspace(0, np.pi, 181)
+    out = S.zwart_powell_sino(r, phi, device=device)
+    out = out.cpu().numpy() if device else out
+    R, P = np.meshgrid(r, phi)
+    np.testing.assert_allclose(out, O.zwart_powell(R, P), rtol=1e-9, atol=1e-12)
+    assert out[90, 50] == pytest.approx(0.75, rel=1e-12)  # r = 0, phi = pi/2: the phi = 0 value by symmetry

@@ -137,3 +137,41 @@ def test_oracle_helix_shift_sign():
     ig2 = dict(ig, offsets=(0.0, 0.0, 0.25 + c / 0.8))
     np.testing.assert_allclose(shifted, O.cbct_back(proj, rg, ig2), rtol=1e-12, atol=1e-12)
     np.testing.assert_array_equal(O.cbct_back(proj, rg, ig, zs=None), O.cbct_back(proj, rg, ig))
+
+
+def test_zwart_powell_known_answers():
+    """test/sys2/zwart_powell.jl:11-13 -- zwart_powell(0, 0) == 0.75, zwart_powell(0, pi/4)
+    ~ 1/sqrt(2) -- from the library and the oracle, and library == oracle on the test grid."""
+    assert S.zwart_powell(0, 0) == 0.75
+    assert S.zwart_powell(0, np.pi / 4) == pytest.approx(1 / np.sqrt(2), rel=1e-12)
+    assert O.zwart_powell(0, 0) == pytest.approx(0.75, rel=1e-14)
+    r = np.linspace(-1, 1, 101) * 2
+    phi = np.linspace(0, np.pi, 181)
+    R, P = np.meshgrid(r, phi)
+    np.testing.assert_allclose(S.zwart_powell(R, P), O.zwart_powell(R, P), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("case", [
+    dict(g=dict(kind="par", nb=64, d=0.7, offset=0.25, na=10, orbit=180.0), ig=dict(dims=(40, 30), deltas=(0.5, 0.6))),
+    dict(g=dict(kind="arc", nb=888, d=1.0239, offset=1.25, na=10, orbit=360.0, dsd=949.075, dod=408.075,
+                source_offset=0.0), ig=dict(dims=(512, 512), deltas=(0.9766, 0.9766))),
+    dict(g=dict(kind="flat", nb=910, d=1.0239, offset=0.0, na=10, orbit=360.0, dsd=949.0, dod=408.0,
+                source_offset=0.0), ig=dict(dims=(256, 200), deltas=(2.0, 2.0))),
+    dict(g=C.ct("flat", offset_s=0.25), ig=dict(dims=(16, 14, 12), deltas=(1.0, 1.1, 0.9))),
+    dict(g=C.ct("arc"), ig=dict(dims=(20, 20, 8), deltas=(2.0, 2.0, 1.0))),
+])
+def test_footprint_size(case):
+    """footprint_size (footprint.jl:19-36) from the library against the oracle restatement."""
+    g, ig = case["g"], case["ig"]
+    got = S.footprint_size(C.to_geom(g), C.to_image(ig))
+    assert got == O.footprint_size(g, ig)
+    assert got > 0
+
+
+def test_footprint_size_bad_dso():
+    """rfov > 0.99 dso throws "bad dso" (footprint.jl:28, :34)."""
+    g = C.ct("flat", dsd=40.0, dod=10.0)  # dso 30 < rfov 40
+    with pytest.raises(S.SinogramsError, match="bad dso"):
+        S.footprint_size(C.to_geom(g), C.to_image(dict(dims=(80, 80, 4), deltas=(1.0, 1.0, 1.0))))
+    with pytest.raises(ValueError, match="bad dso"):
+        O.footprint_size(g, dict(dims=(80, 80, 4), deltas=(1.0, 1.0, 1.0)))
