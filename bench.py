@@ -62,6 +62,24 @@ def _peaks():
         return {}
 
 
+def _filter_roofline(form, peaks):
+    """Tensor-core work of the ramp filter (split-BF16 GEMM on first differences): 2 x rows x
+    K x N x products, K = ns rounded up to 32, N = the output columns the MMAs compute
+    (256-column blocks, the last rounded up to 16), 6 products for FP32 storage (3 pieces)
+    and 3 for BF16 storage (2 pieces).  The stage time includes the split pass."""
+    ns, rows = GEOM["ns"], GEOM["nt"] * GEOM["na"]
+    nout = form["plan"].info()["pitch"]
+    k = -(-ns // 32) * 32
+    n = sum(min(256, -(-(nout - n0) // 16) * 16) for n0 in range(0, nout, 256))
+    products = 3 if form["plan"].storage == "bf16" else 6
+    flops = 2.0 * rows * k * n * products
+    achieved = flops / (form["filter_ms"] / 1e3) / 1e12
+    peak = peaks.get("bf16_tflops")
+    return {"bound": "tensor", "kernel": "split_rows_kernel + filter_gemm_kernel", "achieved": achieved,
+            "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if peak else None,
+            "tensor_flops_per_launch": flops, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
+
+
 def _traffic_from_profile(name: str):
     """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
     (a line 'traffic_bytes_per_launch: N'), or None."""
@@ -230,6 +248,7 @@ def run_ours(args):
                                     "achieved_tflops": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12,
                                     "peak_tflops_nominal": NOMINAL_FP32_TFLOPS,
                                     "frac": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12 / NOMINAL_FP32_TFLOPS}},
+        "filter_roofline": _filter_roofline(forms[head], peaks),
         "plan": forms[head]["plan"].info(),
         "gpu_launches": f["gpu_launches"],
         "clocks": f["clocks"],
