@@ -6,18 +6,22 @@
 // apodizing window (src/fbp/window.jl).  Its last layer starts at zero, so an untrained
 // filter is exactly the plain ramp.
 //
-// Kernels (hand-written; BF16 weights, FP32 activations and accumulation):
+// Training kernels (hand-written; BF16 weights, FP32 activations and accumulation):
 //   conv_fwd      y[r,co,t] = b[co] + sum_{ci,k} W[co,ci,k] x[r,ci,t+k-4]  (+ GELU)
 //   conv_fwd_c1   the same for one output channel
 //   (data gradient = conv_fwd with the transposed, flipped weights)
 //   conv_wgrad    dW[co,ci,k] = sum_{r,t} g[r,co,t] x[r,ci,t+k-4], db[co] = sum g
 //   gelu_bwd, loss (MSE on the residual), adam
 // Activations are (rows, channels, L) with L = detector samples, zero padded by 4.
+//
+// Inference (sgb_lf_apply) runs the whole network in one persistent kernel, lf_tc_fused,
+// with the three 32 -> 32 layers on the tcgen05 tensor cores (see the comment above it).
 #include <cmath>
 #include <cstring>
 #include <vector>
 
 #include "sgb_common.cuh"
+#include "sgb_tc.cuh"
 
 namespace sgb {
 
@@ -212,11 +216,220 @@ __global__ void scale_copy(const float *__restrict__ a, float s, float *__restri
         b[i] = a[i] * s;
 }
 
-__global__ void residual_out(const float *__restrict__ z, const float *__restrict__ o, float s, float *__restrict__ y,
-                             long long n) {
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        y[i] = z[i] + s * o[i];
+
+
+// ------------------------------------------------------- inference on tcgen05
+// The three 32 -> 32 layers of the inference forward run on the tensor cores as an
+// implicit GEMM per tile of 128 positions of one row: D[t, co] = sum_{k, ci} X[t+k-4, ci]
+// W[co, ci, k], M = 128 positions (TMEM lanes), N = 32 output channels, K = 9 taps x 32
+// input channels.  Activations travel between layers position-major, [row][L + 8][32]
+// BF16 with 4 zero positions of padding at each end of a row, as two BF16 pieces
+// (hi = bf16(a), lo = bf16(a - hi)); the weights are BF16 exactly, so D accumulates
+// hi*W + lo*W in FP32 and keeps the activations to ~16 bits.
+//
+// In shared memory a tile's 136 input positions are stored channel-group-major,
+// [piece][ch / 8][position][8], i.e. the canonical no-swizzle K-major layout (8x16-byte
+// core matrices, SBO = 128 B between 8-position groups, LBO = 136 x 16 B between channel
+// groups).  Tap k of the convolution is then the same operand with its start address
+// advanced by k positions (16 B), so one staged tile serves all nine taps.  The weights
+// are staged the same way, [tap][ch / 8][co][8].
+constexpr int kTM = 128, kTPos = kTM + 2 * kPad;
+constexpr int kTcThreads = 128;
+constexpr int kTcABytes = 2 * (kC / 8) * kTPos * 16;  // two pieces
+constexpr int kTcWBytes = kK * (kC / 8) * kC * 16;
+
+__device__ __forceinline__ uint64_t sdesc_k_none(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           ((uint64_t)1 << 46);
 }
+
+// one position's 32 channels, split hi/lo, into a channel-group-major activation buffer
+__device__ __forceinline__ void store_split_cg(uint8_t *A, int pos, const float (&v)[32]) {
+#pragma unroll
+    for (int cg = 0; cg < kC / 8; cg++) {
+        uint32_t h[4], l[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            __nv_bfloat162 a = __floats2bfloat162_rn(v[cg * 8 + 2 * j], v[cg * 8 + 2 * j + 1]);
+            const float2 af = __bfloat1622float2(a);
+            __nv_bfloat162 b = __floats2bfloat162_rn(v[cg * 8 + 2 * j] - af.x, v[cg * 8 + 2 * j + 1] - af.y);
+            h[j] = *reinterpret_cast<uint32_t *>(&a);
+            l[j] = *reinterpret_cast<uint32_t *>(&b);
+        }
+        *reinterpret_cast<uint4 *>(A + (cg * kTPos + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// where each layer's BF16 weights and FP32 bias start in the parameter arrays
+struct LayerWeights {
+    int base[kLayers], bias[kLayers];
+};
+
+// W (cout, cin, 9) BF16 -> [tap][ci / 8][co][ci % 8] for one 32 -> 32 layer
+__global__ void lf_tc_weights(const __nv_bfloat16 *__restrict__ W, __nv_bfloat16 *__restrict__ Wp) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kK * kC * kC; i += gridDim.x * blockDim.x) {
+        const int j = i % 8, co = (i / 8) % kC, cg = (i / (8 * kC)) % (kC / 8), tap = i / (kC * kC);
+        Wp[i] = W[(co * kC + cg * 8 + j) * kK + tap];
+    }
+}
+
+// The whole inference network for tiles of one row, fused: a persistent CTA stages every
+// layer's weights once, then per tile computes layer 0 (SIMT) into a shared-memory
+// activation buffer, the three 32 -> 32 layers on the tensor cores (ping-pong buffers,
+// the operand layout described above), and the last layer with the residual.
+// A tile's window is 136 positions t = ts - 16 + p; each layer invalidates 4 positions at
+// each edge, so the 104 positions p in [16, 120) come out exact.  Activations at t outside
+// [0, L) are written as zeros, the zero padding every layer of the network sees.
+constexpr int kFOut = 104;            // valid outputs per tile
+constexpr int kFZ = kTPos + 2 * kPad;  // z window: t in [ts - 20, ts + 124)
+constexpr size_t kFusedSmem = 3 * (size_t)kTcWBytes + 2 * (size_t)kTcABytes +
+                              sizeof(float) * (2 * kC * kK + 4 * kC + 1 + kFZ) + 64;
+
+__global__ void __launch_bounds__(kTcThreads) lf_tc_fused(const float *__restrict__ z, float s,
+                                                          const __nv_bfloat16 *__restrict__ wb, LayerWeights lw,
+                                                          const __nv_bfloat16 *__restrict__ wp,
+                                                          const float *__restrict__ p, float *__restrict__ y,
+                                                          long long R, int L, int *err) {
+    extern __shared__ __align__(128) uint8_t fsm[];
+    uint8_t *Wl = fsm;                                   // [3][kTcWBytes]
+    uint8_t *Ab = Wl + 3 * kTcWBytes;                    // [2][kTcABytes]
+    float *w0 = reinterpret_cast<float *>(Ab + 2 * kTcABytes);  // [32][9]
+    float *w4 = w0 + kC * kK;                            // [32][9]
+    float *bias = w4 + kC * kK;                          // [4][32] + [1]
+    float *zw = bias + 4 * kC + 1;                       // [kFZ]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(((uintptr_t)(zw + kFZ) + 7) & ~uintptr_t(7));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float inv_s = 1.f / s;  // the network sees z / s
+    for (int i = tid; i < 3 * kTcWBytes / 16; i += kTcThreads)
+        reinterpret_cast<uint4 *>(Wl)[i] = reinterpret_cast<const uint4 *>(wp)[i];
+    for (int i = tid; i < kC * kK; i += kTcThreads) {
+        w0[i] = __bfloat162float(wb[lw.base[0] + i]);
+        w4[i] = __bfloat162float(wb[lw.base[4] + i]);
+    }
+    for (int i = tid; i < 4 * kC + 1; i += kTcThreads) bias[i] = p[lw.bias[min(i / kC, 4)] + (i < 4 * kC ? i % kC : 0)];
+    if (tid == 0) {
+        dev::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 32);
+        tc::tmem_relinquish();
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *slot;
+    const uint32_t ab0 = dev::smem_u32(Ab), wl0 = dev::smem_u32(Wl);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(kTM, kC);
+    const int tpr = (L + kFOut - 1) / kFOut;
+    const long long ntiles = R * tpr;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const long long r = tile / tpr;
+        const int ts = (int)(tile % tpr) * kFOut;  // window position p <-> t = ts - 16 + p
+        const float *zr = z + r * L;
+        for (int j = tid; j < kFZ; j += kTcThreads) {
+            const int t = ts - 20 + j;
+            zw[j] = (t >= 0 && t < L) ? zr[t] : 0.f;
+        }
+        __syncthreads();
+        // layer 0 (1 -> 32, GELU) on all 136 window positions, into buffer 0
+        for (int pp = tid; pp < kTPos; pp += kTcThreads) {
+            const int t = ts - 16 + pp;
+            float v[kC];
+#pragma unroll
+            for (int co = 0; co < kC; co++) {
+                float acc = bias[co];
+#pragma unroll
+                for (int k = 0; k < kK; k++) acc = fmaf(w0[co * kK + k], zw[pp + k] * inv_s, acc);
+                v[co] = (t >= 0 && t < L) ? gelu(acc) : 0.f;
+            }
+            store_split_cg(Ab, pp, v);
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        int cur = 0;
+        for (int l = 0; l < 3 && ok; l++, cur ^= 1) {
+            if (tid == 0) {
+                tc::fence_after_sync();
+                int n = 0;
+                for (int piece = 0; piece < 2; piece++)
+                    for (int k = 0; k < kK; k++)
+                        for (int ks = 0; ks < kC / 16; ks++, n++) {
+                            const uint64_t ad = sdesc_k_none(
+                                ab0 + cur * kTcABytes + ((piece * (kC / 8) + 2 * ks) * kTPos + k) * 16, kTPos * 16, 128);
+                            const uint64_t bd =
+                                sdesc_k_none(wl0 + l * kTcWBytes + ((k * (kC / 8) + 2 * ks) * kC) * 16, kC * 16, 128);
+                            tc::mma_bf16(tbase, ad, bd, idesc, n != 0);
+                        }
+                tc::commit(bar);
+            }
+            int good = 1;
+            if (lane == 0) {
+                const long long c0 = clock64();
+                while (!dev::mbar_try_wait(bar, phase & 1))
+                    if (clock64() - c0 > dev::kWaitBudget) {
+                        atomicOr(err, 1);
+                        good = 0;
+                        break;
+                    }
+            }
+            good = __shfl_sync(0xffffffffu, good, 0);
+            phase++;
+            tc::fence_after_sync();
+            if (good) {
+                float v[32];
+                tc::ld32(tbase + ((uint32_t)(32 * warp) << 16), v);
+                const int pp = 4 + 32 * warp + lane;  // output row m = pp - 4
+                const int t = ts - 16 + pp;
+                const float *bl = bias + (l + 1) * kC;
+#pragma unroll
+                for (int co = 0; co < kC; co++) v[co] = (t >= 0 && t < L) ? gelu(v[co] + bl[co]) : 0.f;
+                store_split_cg(Ab + (cur ^ 1) * kTcABytes, pp, v);
+            }
+            if (!__syncthreads_and(good)) ok = false;  // also orders the TMEM reads before the next MMAs
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+        if (!ok) break;
+        // last layer (32 -> 1) and the residual on the 104 exact positions
+        if (tid < kFOut) {
+            const int pp = 16 + tid, t = ts + tid;
+            if (t < L) {
+                const uint8_t *A = Ab + cur * kTcABytes;
+                float acc = bias[4 * kC];
+#pragma unroll
+                for (int k = 0; k < kK; k++) {
+                    const int row = pp - 4 + k;
+#pragma unroll
+                    for (int cg = 0; cg < kC / 8; cg++) {
+                        const uint4 h = *reinterpret_cast<const uint4 *>(A + (cg * kTPos + row) * 16);
+                        const uint4 q = *reinterpret_cast<const uint4 *>(A + ((kC / 8 + cg) * kTPos + row) * 16);
+                        const uint32_t hv[4] = {h.x, h.y, h.z, h.w}, qv[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                        for (int j = 0; j < 4; j++) {
+                            const float a0 = __uint_as_float(hv[j] << 16) + __uint_as_float(qv[j] << 16);
+                            const float a1 = __uint_as_float(hv[j] & 0xFFFF0000u) + __uint_as_float(qv[j] & 0xFFFF0000u);
+                            acc = fmaf(w4[(cg * 8 + 2 * j) * kK + k], a0, acc);
+                            acc = fmaf(w4[(cg * 8 + 2 * j + 1) * kK + k], a1, acc);
+                        }
+                    }
+                }
+                y[r * L + t] = zw[pp + 4] + s * acc;
+            }
+        }
+        __syncthreads();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 32);
+}
+
 
 // Adam on the FP32 master parameters; refreshes the BF16 weights and the transposed,
 // flipped BF16 weights the data-gradient convolution uses.
@@ -269,6 +482,9 @@ struct sgb_lf {
     DevBuf act[kLayers + 1], pre[kLayers], ga, gb, gz;
     long long cap_rows = 0;
     int cap_L = 0;
+    // tensor-core inference: packed weights of the 32 -> 32 layers (valid for twp_step), error flag
+    DevBuf twp, terr;
+    long long twp_step = -1;
 };
 
 namespace {
@@ -313,6 +529,39 @@ int lf_forward(sgb_lf *F, long long R, int L, cudaStream_t st) {
         F->act[kLayers - 1].as<float>(), wb + F->wbase[kLayers - 1], p + F->off.b[kLayers - 1],
         F->act[kLayers].as<float>(), L, true);
     return after_launch("conv_fwd_c1");
+}
+
+int lf_tc_workspace(sgb_lf *F) {
+    SGB_TRY(F->twp.reserve(sizeof(__nv_bfloat16) * 3 * kK * kC * kC));
+    SGB_TRY(F->terr.reserve(sizeof(int)));
+    return SGB_OK;
+}
+
+// Inference forward with the 32 -> 32 layers on the tensor cores; writes y = z + s net(z/s).
+int lf_forward_tc(sgb_lf *F, const float *zdev, long long R, int L, float *ydev, cudaStream_t st) {
+    SGB_TRY(lf_tc_workspace(F));
+    const __nv_bfloat16 *wb = F->wb.as<__nv_bfloat16>();
+    const float *p = F->p.as<float>();
+    __nv_bfloat16 *wp = F->twp.as<__nv_bfloat16>();
+    SGB_CUDA(cudaMemsetAsync(F->terr.p, 0, sizeof(int), st));
+    if (F->twp_step != F->step) {  // repack after training steps only
+        for (int l = 1; l <= 3; l++) lf_tc_weights<<<9, 1024, 0, st>>>(wb + F->wbase[l], wp + (l - 1) * kK * kC * kC);
+        SGB_TRY(after_launch("lf_tc_weights"));
+        F->twp_step = F->step;
+    }
+    LayerWeights lw;
+    for (int l = 0; l < kLayers; l++) {
+        lw.base[l] = F->wbase[l];
+        lw.bias[l] = F->off.b[l];
+    }
+    const long long ntiles = R * ((L + kFOut - 1) / kFOut);
+    int dev = 0, sms = 0;
+    SGB_CUDA(cudaGetDevice(&dev));
+    SGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    SGB_CUDA(cudaFuncSetAttribute(lf_tc_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem));
+    const unsigned grid = (unsigned)std::min<long long>(ntiles, 2ll * sms);
+    lf_tc_fused<<<grid, kTcThreads, kFusedSmem, st>>>(zdev, F->scale, wb, lw, wp, p, ydev, R, L, F->terr.as<int>());
+    return after_launch("lf_tc_fused");
 }
 
 // backward from the gradient wrt the net output (in gz); accumulates parameter grads in F->g
@@ -429,24 +678,26 @@ int sgb_lf_get_params(const sgb_lf *F, float *params, float *scale) {
 
 int sgb_lf_apply(sgb_lf *F, const float *z, long long rows, int L, float *y, int flags, void *stream) {
     SGB_REQUIRE(F && z && y && rows > 0 && L > 0, "lf_apply: bad argument");
-    SGB_REQUIRE(rows <= 65535, "learned filter: at most 65535 rows per call");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    SGB_TRY(lf_workspace(F, rows, L));
     DevBuf tz, ty;
-    const float *zdev;
-    SGB_TRY(lf_stage_input(F, z, rows, L, flags, tz, &zdev, st));
-    SGB_TRY(lf_forward(F, rows, L, st));
+    const void *zdev;
+    SGB_TRY(stage_in(z, sizeof(float) * (size_t)rows * L, flags, tz, &zdev, st));
     float *ydev = y;
     if (!(flags & SGB_DEVICE_PTRS)) {
         SGB_TRY(ty.reserve(sizeof(float) * (size_t)rows * L));
         ydev = ty.as<float>();
     }
-    residual_out<<<grid_for(rows * (long long)L), 256, 0, st>>>(zdev, F->act[kLayers].as<float>(), F->scale, ydev,
-                                                                rows * (long long)L);
-    SGB_TRY(after_launch("residual_out"));
+    SGB_TRY(lf_forward_tc(F, static_cast<const float *>(zdev), rows, L, ydev, st));
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(y, ydev, sizeof(float) * (size_t)rows * L, cudaMemcpyDeviceToHost, st));
+    if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
     SGB_CUDA(cudaStreamSynchronize(st));
+    int e = 0;
+    SGB_CUDA(cudaMemcpy(&e, F->terr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        set_error("lf_apply: tensor-core convolution reported a wait timeout");
+        return SGB_ERR_TIMEOUT;
+    }
     return SGB_OK;
 }
 

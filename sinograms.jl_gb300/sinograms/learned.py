@@ -84,8 +84,9 @@ class LearnedFilter:
         d = np.load(path)
         return cls(float(d["scale"]), d["params"])
 
-    def apply(self, z):
-        """y = z + scale * net(z / scale) for rows z of shape (..., L)."""
+    def apply(self, z, sync: bool = True):
+        """y = z + scale * net(z / scale) for rows z of shape (..., L); with CUDA tensors and
+        sync=False the call only enqueues work on the current stream."""
         a = Arr(z)
         L = a.shape[-1]
         R = int(np.prod(a.shape[:-1]))
@@ -95,7 +96,7 @@ class LearnedFilter:
             n = min(65535, R - r0)
             zi = ctypes.c_void_p(a.ptr.value + 4 * r0 * L)
             yi = ctypes.c_void_p(ptr(out).value + 4 * r0 * L)
-            _status(_lib.lib().sgb_lf_apply(self._h, zi, n, L, yi, flags_for(a.device), stream_for(a.device)),
+            _status(_lib.lib().sgb_lf_apply(self._h, zi, n, L, yi, flags_for(a.device, sync), stream_for(a.device)),
                     "lf_apply")
         return out
 
@@ -121,23 +122,23 @@ class LearnedFilter:
 
 # ------------------------------------------------------------------- plan stages
 
-def fbp_filter_rows(plan: FBPNormalPlan, sino):
+def fbp_filter_rows(plan: FBPNormalPlan, sino, sync: bool = True):
     """Weighted, ramp-filtered rows of fbp(plan, sino) (the stage before back-projection)."""
     a = Arr(sino)
     out = torch.empty(a.shape, dtype=torch.float32, device=a.obj.device) if a.device else np.empty(a.shape, np.float32)
     nsl = int(np.prod(a.shape[:-2])) if len(a.shape) > 2 else 1
-    _status(_lib.lib().sgb_fbp_filter_rows(plan.handle, a.ptr, ptr(out), nsl, flags_for(a.device),
+    _status(_lib.lib().sgb_fbp_filter_rows(plan.handle, a.ptr, ptr(out), nsl, flags_for(a.device, sync),
                                            stream_for(a.device)), "fbp_filter_rows")
     return out
 
 
-def fbp_backproject(plan: FBPNormalPlan, filtered):
+def fbp_backproject(plan: FBPNormalPlan, filtered, sync: bool = True):
     """The back-projection stage of fbp(plan, sino) on already filtered rows."""
     a = Arr(filtered)
     shape = tuple(a.shape[:-2]) + tuple(reversed(plan.ig.dims))
     out = torch.empty(shape, dtype=torch.float32, device=a.obj.device) if a.device else np.empty(shape, np.float32)
     nsl = int(np.prod(a.shape[:-2])) if len(a.shape) > 2 else 1
-    _status(_lib.lib().sgb_fbp_backproject(plan.handle, a.ptr, ptr(out), nsl, flags_for(a.device),
+    _status(_lib.lib().sgb_fbp_backproject(plan.handle, a.ptr, ptr(out), nsl, flags_for(a.device, sync),
                                            stream_for(a.device)), "fbp_backproject")
     return out
 

@@ -30,9 +30,27 @@ def test_gradients_match_fp64_oracle(cuda, L):
     lo, go = LO.loss_grad(p.astype(np.float64), z, t, 0.8, bf16_weights=True)
     assert loss == pytest.approx(lo, rel=1e-5)
     assert np.linalg.norm(g - go) / np.linalg.norm(go) < 1e-4
+    # apply is the tensor-core inference path: activations travel as two BF16 pieces
+    # (~16 bits), so it holds 5e-5 where the FP32-activation training forward holds 1e-5
     y = lf.apply(z)
     yo, _ = LO.forward(p.astype(np.float64), z, 0.8)
-    assert np.abs(y - yo).max() <= 1e-5 * np.abs(yo).max()
+    assert np.abs(y - yo).max() <= 5e-5 * np.abs(yo).max()
+
+
+@pytest.mark.parametrize("rows,L", [(3, 37), (130, 200), (90, 888)])
+def test_tensor_core_apply_matches_fp64_oracle(cuda, rows, L):
+    """The inference forward (32 -> 32 layers on tcgen05, activations split hi+lo in BF16)
+    against the FP64 oracle: the learned correction y - z to 1e-4 relative, over partial
+    128-position tiles and rows of one to seven tiles."""
+    rng = np.random.default_rng(rows + L)
+    p = (0.3 * rng.standard_normal(LO.nparams())).astype(np.float32)
+    z = rng.standard_normal((rows, L)).astype(np.float32)
+    lf = LF.LearnedFilter(scale=0.7, params=p)
+    y = lf.apply(z)
+    yo, _ = LO.forward(p.astype(np.float64), z, 0.7)
+    d, do = y.astype(np.float64) - z, yo - z
+    assert np.linalg.norm(d - do) / np.linalg.norm(do) < 1e-4
+    assert np.abs(d - do).max() <= 1e-4 * np.abs(do).max()
 
 
 def test_training_reduces_the_loss(cuda):
