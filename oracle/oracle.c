@@ -280,7 +280,9 @@ void orc_fbp_sino_weight(const double *gam, int nb, double dso, double source_of
  * betas has na entries; views ia = 1:ia_skip:na are used (:121-125). */
 /* cbct_back with a per-view source z (zs_ds[ia] = source_zs[ia] / ds, or NULL for the
  * reference's z_src = 0): t' = mag * (z_ds - source_zs[ia]), the form left commented at
- * cbct-back.jl:188.  With NULL this is exactly cbct_back_fan_voxel. */
+ * cbct-back.jl:188.  With NULL this is exactly cbct_back_fan_voxel.  is_arc: 0 flat,
+ * 1 arc, 2 CtPar (parallel beam, which the reference does not back-project: s' = x_beta,
+ * t' = z, unit weight -- the 2D rule of fbp_back_par extended along the detector rows). */
 int orc_cbct_back_zs(real_t *image, const real_t *proj, int ns, int nt, int na, const double *betas,
                      double dsd, double dso, double ds, double dt, float offset_s, float offset_t,
                      int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
@@ -310,7 +312,11 @@ int orc_cbct_back_zs(real_t *image, const real_t *proj, int ns, int nt, int na, 
             real_t x_beta = x_ds * c_b + y_ds * s_b;              /* :174 */
             real_t y_beta = dso_ds - (-x_ds * s_b + y_ds * c_b);   /* :175 */
             real_t mag, sprime_ds, w2;
-            if (is_arc) {                                          /* :177-186 */
+            if (is_arc == 2) { /* CtPar: the source at infinity, t' = z, unit weight (back-par.jl:447 in 3D) */
+                mag = 1;
+                sprime_ds = x_beta;
+                w2 = 1;
+            } else if (is_arc) {                                   /* :177-186 */
                 real_t r_loop = x_beta;
                 sprime_ds = dsd_ds * atan2(r_loop, y_beta);
                 mag = dsd_ds / y_beta;

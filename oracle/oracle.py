@@ -102,7 +102,7 @@ def t_axis(g) -> np.ndarray:
 
 
 def dso(g) -> float:
-    return float(_f(g, "dsd")) - float(_f(g, "dod"))
+    return float(_f(g, "dsd", 0.0)) - float(_f(g, "dod", 0.0))
 
 
 def gamma(g) -> np.ndarray:
@@ -217,7 +217,11 @@ def fdk_weight_cyl(rg) -> np.ndarray:
 
 
 def fdk_weights(rg) -> np.ndarray:
-    """_fdk_weights, plan3.jl:75-80."""
+    """_fdk_weights, plan3.jl:75-80.  CtPar (no FBP in the reference): the view weights of
+    the equivalent SinoPar, parker_weight_par x dbeta, without a cylinder weight."""
+    if _f(rg, "kind") == "par":
+        pw = parker_weight(rg)
+        return pw.reshape(pw.shape[0], 1, 1) * angle_weight(rg)
     return parker_weight(rg) * fdk_weight_cyl(rg)[None, :, :] * angle_weight(rg)
 
 
@@ -273,10 +277,11 @@ def cbct_back(proj: np.ndarray, rg, ig, ia_skip: int = 1, bits: int = 64, betas=
     m = _mask(ig)
     zsd = None if zs is None else np.ascontiguousarray(np.asarray(zs, np.float64) / float(_f(rg, "ds")))
     _check(lib(bits).orc_cbct_back_zs(
-        _ptr(img), _ptr(proj), ns, nt, na, _ptr(b), _c_double(float(_f(rg, "dsd"))), _c_double(dso(rg)),
+        _ptr(img), _ptr(proj), ns, nt, na, _ptr(b), _c_double(float(_f(rg, "dsd", 0.0))), _c_double(dso(rg)),
         _c_double(float(_f(rg, "ds"))), _c_double(float(_f(rg, "dt"))),
         _c_float(float(_f(rg, "offset_s", 0.0))), _c_float(float(_f(rg, "offset_t", 0.0))),
-        int(_f(rg, "kind") == "arc"), _ptr(xc), _ptr(yc), _ptr(zc), nx, ny, nz, _ptr(m), ia_skip, _ptr(zsd)),
+        {"flat": 0, "arc": 1, "par": 2}[_f(rg, "kind")], _ptr(xc), _ptr(yc), _ptr(zc), nx, ny, nz, _ptr(m), ia_skip,
+        _ptr(zsd)),
         "cbct_back")
     return img
 

@@ -314,7 +314,8 @@ int sgb_plan_fbp_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_f
 static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const sgb_filter_opts *opt,
                           bool tune, sgb_plan **plan) {
     SGB_REQUIRE(rg && ig && plan, "plan_fbp: null argument");
-    SGB_REQUIRE(rg->kind == SGB_ARC || rg->kind == SGB_FLAT, "plan_fbp: CtGeom must be CtFanArc or CtFanFlat");
+    SGB_REQUIRE(rg->kind == SGB_ARC || rg->kind == SGB_FLAT || rg->kind == SGB_PAR,
+                "plan_fbp: CtGeom must be CtFanArc, CtFanFlat or CtPar");
     SGB_REQUIRE(rg->ns > 1 && rg->nt > 1 && rg->na > 1, "plan_fbp: ns, nt, na must exceed 1");
     SGB_REQUIRE(rg->src == SGB_SRC_CIRCLE || rg->src == SGB_SRC_HELIX, "plan_fbp: unknown CtSource %d", rg->src);
     cudaStream_t st = 0;
@@ -324,7 +325,28 @@ static int create_ct_plan(const sgb_ct_geom *rg, const sgb_image_geom *ig, const
     std::vector<double> ar = view_angles(rg->na, rg->orbit, rg->orbit_start);
     int s = plan_common(P, rg->kind, rg->ns, rg->ds, rg->dsd, opt, rg->nt, rg->na, ar.data(), st);
     if (s == SGB_OK) s = plan_image(P, ig, rg->ds, 3, st);
-    if (s == SGB_OK) {  // _fdk_weights = parker .* fdk_weight_cyl .* dbeta (plan3.jl:75-80)
+    if (s == SGB_OK && rg->kind == SGB_PAR) {
+        // CtPar (no FBP in the reference): the view weights of the equivalent SinoPar,
+        // parker_weight_par x dbeta (parker.jl:26-55, plan2.jl:141-145), no cylinder weight
+        sgb_sino_geom sg{};
+        sg.kind = SGB_PAR;
+        sg.nb = rg->ns;
+        sg.d = rg->ds;
+        sg.offset = rg->offset_s;
+        sg.na = rg->na;
+        sg.orbit = rg->orbit;
+        sg.orbit_start = rg->orbit_start;
+        std::vector<float> pk((size_t)rg->ns * rg->na);
+        int n0, n1;
+        s = sgb_parker_weight_sino(&sg, pk.data(), &n0, &n1);
+        if (s == SGB_OK && n1 > 1) {  // (1, na)
+            std::vector<double> a(pk.begin(), pk.begin() + rg->na);
+            s = upload_f32(a.data(), a.size(), 1.0, P->wA, st);
+            P->sAj = 0;
+            P->sAa = 1;
+            P->hasA = true;
+        }
+    } else if (s == SGB_OK) {  // _fdk_weights = parker .* fdk_weight_cyl .* dbeta (plan3.jl:75-80)
         std::vector<float> pk((size_t)rg->ns * rg->na);
         int n0, n2;
         s = sgb_parker_weight_ct(rg, pk.data(), &n0, &n2);
@@ -533,6 +555,7 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     A.dso_ds = (float)((g.dsd - g.dod) / g.ds);
     A.inv_dtds = (float)(g.ds / g.dt);
     A.is_arc = g.kind == SGB_ARC;
+    A.is_par = g.kind == SGB_PAR;
     A.bf16 = P->storage == SGB_STORE_BF16;
     SGB_TRY(launch_fdk_back(A, st));
     P->mark(2, st);

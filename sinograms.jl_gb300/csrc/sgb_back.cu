@@ -29,7 +29,8 @@ __global__ void view_trig_kernel(const double *__restrict__ betas, int nv, int i
 constexpr int kBX = 32, kBY = 4;  // FDK CTA: 32 x 4 columns
 constexpr int kVChunk = 1024;     // views staged in shared memory per pass
 
-template <typename TP, bool ARC, int kZ>
+// GEO: 0 CtFanFlat, 1 CtFanArc, 2 CtPar (3D parallel beam: s' = x_beta, t' = z, unit weight)
+template <typename TP, int GEO, int kZ>
 __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
     __shared__ float2 trig_s[kVChunk];
     __shared__ float zs_s[kVChunk];  // source z / ds per view (0 for a circular orbit)
@@ -67,16 +68,22 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
             const float zs = zs_s[vi];
             const float sb = sc.x, cb = sc.y;
             const float xb = fmaf(x, cb, y * sb);                    // cbct-back.jl:174
-            const float yb = A.dso_ds - fmaf(-x, sb, y * cb);        // :175
             float mag, sp, w2;
-            if (ARC) {                                               // :177-181
-                sp = A.dsd_ds * atan2f(xb, yb);
-                mag = __fdividef(A.dsd_ds, yb);
-                w2 = __fdividef(A.dsd_ds * A.dsd_ds, fmaf(xb, xb, yb * yb));
-            } else {                                                 // :183-185
-                mag = __fdividef(A.dsd_ds, yb);
-                sp = mag * xb;
-                w2 = mag * mag;
+            if (GEO == 2) {  // parallel beam: the fan map with the source at infinity (back-par.jl:447)
+                mag = 1.f;
+                sp = xb;
+                w2 = 1.f;
+            } else {
+                const float yb = A.dso_ds - fmaf(-x, sb, y * cb);    // :175
+                if (GEO == 1) {                                      // :177-181
+                    sp = A.dsd_ds * atan2f(xb, yb);
+                    mag = __fdividef(A.dsd_ds, yb);
+                    w2 = __fdividef(A.dsd_ds * A.dsd_ds, fmaf(xb, xb, yb * yb));
+                } else {                                             // :183-185
+                    mag = __fdividef(A.dsd_ds, yb);
+                    sp = mag * xb;
+                    w2 = mag * mag;
+                }
             }
             const float bs = sp + A.ws;                              // :191
             const float fis = floorf(bs);
@@ -112,12 +119,12 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
     }
 }
 
-template <typename TP, bool ARC>
+template <typename TP, int GEO>
 int launch_fdk_z(const FdkArgs &A, cudaStream_t st) {
     constexpr int kZ = 8;
     dim3 block(kBX, kBY);
     dim3 grid(floor_div_up(A.nx, kBX), floor_div_up(A.ny, kBY), floor_div_up(A.nz, kZ));
-    fdk_back_kernel<TP, ARC, kZ><<<grid, block, 0, st>>>(A);
+    fdk_back_kernel<TP, GEO, kZ><<<grid, block, 0, st>>>(A);
     return after_launch("fdk_back_kernel");
 }
 
@@ -188,8 +195,12 @@ int launch_view_trig(const double *betas_dev, int na, int ia_skip, float2 *trig,
 
 int launch_fdk_back(const FdkArgs &A, cudaStream_t st) {
     if (A.nx <= 0 || A.ny <= 0 || A.nz <= 0) return SGB_OK;
-    if (A.bf16) return A.is_arc ? launch_fdk_z<__nv_bfloat16, true>(A, st) : launch_fdk_z<__nv_bfloat16, false>(A, st);
-    return A.is_arc ? launch_fdk_z<float, true>(A, st) : launch_fdk_z<float, false>(A, st);
+    const int geo = A.is_par ? 2 : (A.is_arc ? 1 : 0);
+    if (A.bf16)
+        return geo == 2 ? launch_fdk_z<__nv_bfloat16, 2>(A, st)
+                        : (geo == 1 ? launch_fdk_z<__nv_bfloat16, 1>(A, st) : launch_fdk_z<__nv_bfloat16, 0>(A, st));
+    return geo == 2 ? launch_fdk_z<float, 2>(A, st)
+                    : (geo == 1 ? launch_fdk_z<float, 1>(A, st) : launch_fdk_z<float, 0>(A, st));
 }
 
 int launch_back2(const Back2Args &A, cudaStream_t st) {

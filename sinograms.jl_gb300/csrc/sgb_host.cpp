@@ -364,6 +364,10 @@ int sgb_footprint_size_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, float
     SGB_REQUIRE(rg && ig && size, "footprint_size: null argument");
     SGB_REQUIRE(ig->ndim == 3, "footprint_size: CtGeom needs a 3D ImageGeom");
     const double ratio = footprint_di(ig) / rg->ds;  // :13
+    if (rg->kind == SGB_PAR) {
+        *size = (float)ratio;  // CtPar, :23
+        return SGB_OK;
+    }
     double smax = 0;
     for (int i = 0; i < rg->ns; i++)
         smax = std::fmax(smax, std::fabs(rg->ds * (i - ((rg->ns - 1) / 2.0 + rg->offset_s))));  // _s, ct-geom.jl:148

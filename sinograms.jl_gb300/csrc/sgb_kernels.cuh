@@ -66,6 +66,7 @@ struct FdkArgs {
     float ws, wt;          // (ns+1)/2 + offset_s, (nt+1)/2 + offset_t (1-based)
     float dsd_ds, dso_ds, inv_dtds;
     int is_arc;
+    int is_par;            // CtPar: parallel beam (s' = x_beta, t' = z, unit weight)
     int bf16;
 };
 int launch_fdk_back(const FdkArgs &A, cudaStream_t st);

@@ -158,7 +158,14 @@ def fbp_sino_weight(rg) -> np.ndarray:
 
 
 def fdk_view_weight(rg) -> np.ndarray:
-    """_fdk_weights(rg), plan3.jl:75-80 (numpy (1|na, nt, ns))."""
+    """_fdk_weights(rg), plan3.jl:75-80 (numpy (1|na, nt, ns)).  CtPar, which the reference
+    does not reconstruct, takes the view weights of the equivalent SinoPar (no cylinder
+    weight)."""
+    from .geom import CtPar, SinoPar
+    if isinstance(rg, CtPar):
+        sp = SinoPar(nb=rg.ns, d=rg.ds, offset=rg.offset_s, na=rg.na, orbit=rg.orbit, orbit_start=rg.orbit_start)
+        pw = parker_weight(sp)
+        return pw.reshape(pw.shape[0], 1, 1) * _angle_weights(_ar(rg))
     return parker_weight(rg) * fdk_weight_cyl(rg)[None] * _angle_weights(_ar(rg))
 
 

@@ -171,13 +171,42 @@ class CtFanFlat(_CtFan):
     kind = "flat"
 
 
+@dataclass(frozen=True)
+class CtPar:
+    """3D parallel-beam geometry (type3.jl:102-115, constructor defaults :211-230).  The
+    reference defines it but has no FBP for it; plan_fbp(CtPar, ig) + fdk here reconstruct
+    it with the flat ramp, SinoPar's view weights and a voxel-driven back-projection with
+    s = x cos(b) + y sin(b) and t = z."""
+    ns: int = 128
+    nt: int = 64
+    ds: float = 1.0
+    dt: float | None = None
+    offset_s: float = 0.0
+    offset_t: float = 0.0
+    na: int = 60
+    orbit: float = 180.0
+    orbit_start: float = 0.0
+    kind = "par"
+    src = CtSourceCircle()
+    source_offset = 0.0
+    dsd = 0.0
+    dod = 0.0
+
+    def __post_init__(self):
+        object.__setattr__(self, "offset_s", _f32(self.offset_s))
+        object.__setattr__(self, "offset_t", _f32(self.offset_t))
+        if self.dt is None:
+            object.__setattr__(self, "dt", self.ds)
+
+
 SinoGeom = (SinoPar, SinoFanArc, SinoFanFlat)
 SinoFan = (SinoFanArc, SinoFanFlat)
 CtFan = (CtFanArc, CtFanFlat)
+CtGeom = (CtFanArc, CtFanFlat, CtPar)
 
 
 def is_ct(rg) -> bool:
-    return isinstance(rg, CtFan)
+    return isinstance(rg, CtGeom)
 
 
 def dims(rg):
@@ -245,7 +274,9 @@ def downsample(rg, down: int):
 
 
 def _zfov(rg) -> float:
-    """_zfov(rg::CtFan), ct-geom.jl:120."""
+    """_zfov(rg), ct-geom.jl:119-121."""
+    if isinstance(rg, CtPar):
+        return rg.nt * rg.dt
     return _dso(rg) / rg.dsd * rg.nt * rg.dt
 
 

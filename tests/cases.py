@@ -47,6 +47,10 @@ ARC_SHORT = dict(rg=short(_ARC, 48), ig=PAR["ig"], window="none")
 FLAT = dict(rg=dict(_ARC, kind="flat"), ig=PAR["ig"], window="hamming")
 BDD = dict(DSD=300.0, DS0=180.0, pSize=2.0, dSize=2.3, nPix=32, nDet=40, angle=np.arange(24) * (2 * math.pi / 24))
 FILTER_WRAP = dict(nb=24, npad=32, extra=3, rows=5)
+# 3D parallel beam (CtPar, type3.jl:102-115): 200 degrees so the Parker ramp of SinoPar applies
+CT_PAR = dict(rg=dict(kind="par", ns=40, nt=24, ds=1.0, dt=1.2, offset_s=0.25, offset_t=-0.5, na=40, orbit=200.0,
+                      orbit_start=10.0),
+              ig=dict(dims=(24, 22, 10), deltas=(1.1, 1.0, 0.9), offsets=(0.3, -0.2, 0.1)))
 # helical source (CtSourceHelix, ct-source.jl:29-56): half a zFOV of travel per turn,
 # centred so the source z sweeps the image's z extent
 HELIX = dict(rg=ct("flat", src="helix", pitch=0.5, source_z0=-5.4, offset_s=0.25),
@@ -68,6 +72,10 @@ def to_geom(g):
     if "ns" in g:
         if g.pop("src", "circle") == "helix":
             g["src"] = S.CtSourceHelix(pitch=g.pop("pitch"), source_z0=g.pop("source_z0"))
+        if kind == "par":
+            for k in ("dsd", "dod", "source_offset"):
+                g.pop(k, None)
+            return S.CtPar(**g)
         return (S.CtFanArc if kind == "arc" else S.CtFanFlat)(**g)
     if kind == "par":
         return S.SinoPar(**g)

@@ -278,3 +278,35 @@ def test_zwart_powell_sino_gpu(cuda, device):
     R, P = np.meshgrid(r, phi)
     np.testing.assert_allclose(out, O.zwart_powell(R, P), rtol=1e-9, atol=1e-12)
     assert out[90, 50] == pytest.approx(0.75, rel=1e-12)  # r = 0, phi = pi/2: the phi = 0 value by symmetry
+
+
+@pytest.mark.parametrize("storage", ["f32", "bf16"])
+def test_ctpar_fbp_against_oracle(cuda, storage):
+    """CtPar (3D parallel beam; the reference defines it but does not reconstruct it):
+    flat ramp, SinoPar's Parker x dbeta view weights, s = x cos + y sin, t = z."""
+    c = C.CT_PAR
+    rng = np.random.default_rng(11)
+    g = c["rg"]
+    proj = rng.standard_normal((g["na"], g["nt"], g["ns"])).astype(np.float32)
+    ref = O.fdk(g, c["ig"], proj)
+    plan = S.plan_fbp(C.to_geom(g), C.to_image(c["ig"]), storage=storage)
+    # white-noise rows: the BF16 storage rounding (2^-9) shows through undamped, hence 4e-3
+    close(S.fdk(plan, proj), ref, *((RTOL_RMSE, MAX_REL) if storage == "f32" else (4e-3, 2e-2)))
+    assert S.footprint_size(C.to_geom(g), C.to_image(c["ig"])) == pytest.approx(np.hypot(1.1, 1.0) / 1.0, rel=1e-6)
+
+
+def test_ctpar_slices_equal_sinopar_fbp(cuda):
+    """With the image z grid on the detector rows, a CtPar reconstruction's slice is the 2D
+    SinoPar FBP (fbp.jl:24-68) of that detector row (t-lerp weight 0)."""
+    # ds = dt keeps bt = z / ds + wt exact on the rows (an FP32 product could land just below
+    # a row and drop it by the whole-tap rule)
+    rg = S.CtPar(ns=48, nt=12, ds=1.0, dt=1.0, offset_s=0.25, offset_t=0.0, na=36, orbit=180.0)
+    ig = S.ImageGeom((30, 26, 12), (0.7, 0.75, 1.0))
+    rng = np.random.default_rng(5)
+    proj = rng.standard_normal((rg.na, rg.nt, rg.ns)).astype(np.float32)
+    vol = S.fdk(S.plan_fbp(rg, ig), proj)
+    sp = S.SinoPar(nb=48, d=1.0, offset=0.25, na=36, orbit=180.0)
+    plan2 = S.plan_fbp(sp, S.ImageGeom((30, 26), (0.7, 0.75)))
+    for j in range(rg.nt - 1):  # the last row is dropped by the whole-tap rule 1 <= floor(bt) < nt
+        close(vol[j], S.fbp(plan2, np.ascontiguousarray(proj[:, j, :])))
+    assert np.all(vol[rg.nt - 1] == 0)
