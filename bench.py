@@ -46,6 +46,23 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, ws: int, device) -> float:
+    """The slowest rank's value (the timing contract: max over ranks); identity when ws == 1.
+    `device` holds the reduction tensor: "cuda" under NCCL, "cpu" under gloo."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(ws: int, units_per_rank: float, steps: int, max_ms: float) -> float:
+    """Whole-job throughput of independent replicas: all ranks' units / the slowest rank's time."""
+    return ws * units_per_rank * steps / (max_ms / 1e3)
+
+
 def _phantom():
     import sinograms as S
     return S.random_ellipsoids(30, 3, 100.0, 50.0, axes=(3.0, 60.0), dens=(-0.3, 1.0))
@@ -191,12 +208,8 @@ def run_ours(args):
         launches = S.launch_count() - l0
         clocks = sampler.stop()
         barrier()
-        ms = e0.elapsed_time(e1)
-        if ws > 1:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        forms[storage] = dict(ms_per_step=ms / args.steps, value=ws * upd * args.steps / (ms / 1e3),
+        ms = max_over_ranks(e0.elapsed_time(e1), ws, "cuda")
+        forms[storage] = dict(ms_per_step=ms / args.steps, value=replica_throughput(ws, upd, args.steps, ms),
                               filter_ms=float(np.mean(fms)), back_ms=float(np.mean(bms)), gpu_launches=launches,
                               clocks=clocks, plan=plan)
         outs[storage] = img
@@ -215,11 +228,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         S.fdk(plan, hp, out=hi)  # blocking call: copies in, computes, copies out
-    e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
     barrier()
 
     peaks = _peaks()
@@ -237,7 +246,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (566 MB projections per step)", "parallelism": f"replicas x{ws}"},
         "forms": {k: {"value": v["value"], "ms_per_step": v["ms_per_step"], "filter_ms": v["filter_ms"],
                       "back_ms": v["back_ms"]} for k, v in forms.items()},
-        "e2e": {"value": ws * upd * args.steps / e2e_s, "unit": UNIT,
+        "e2e": {"value": replica_throughput(ws, upd, args.steps, e2e_s * 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": proj.numel() * 4, "d2h_bytes_per_step": nvox * 4},
         "roofline": {"bound": "hbm", "kernel": "fdk_tma_kernel", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": (achieved / hbm) if hbm else None,

@@ -266,6 +266,12 @@ SGB_API int sgb_lf_train_step(sgb_lf *lf, const float *z, const float *target, l
                               float lr, double *loss, int flags, void *stream);
 SGB_API int sgb_lf_destroy(sgb_lf *lf);
 
+/* ------------------------------------------------------ failure detection */
+/* Runs one kernel whose mbarrier wait can never complete, bounded by budget_cycles (1e3 ..
+ * the library's ~2 s budget): the bounded-wait error path of every TMA / tensor-core
+ * kernel.  Returns SGB_ERR_TIMEOUT with the expired-wait message; the context stays usable. */
+SGB_API int sgb_selftest_wait_timeout(long long budget_cycles, void *stream);
+
 /* ------------------------------------------------- sys2 geometry helpers */
 /* footprint_size(st, ig), src/sys2/footprint.jl:19-36: maximum footprint of a pixel in
  * detector samples (Float32).  Arc/flat fans return SGB_ERR_GEOM ("bad dso") when the

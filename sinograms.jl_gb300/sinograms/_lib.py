@@ -63,6 +63,7 @@ _SIGS = {
     "sgb_footprint_size_ct": (c_int, [P, P, P]),
     "sgb_zwart_powell": (c_double, [c_double, c_double]),
     "sgb_zwart_powell_sino": (c_int, [P, c_int, P, c_int, P, c_int, P]),
+    "sgb_selftest_wait_timeout": (c_int, [c_ll, P]),
     "sgb_fbp_sino_weight": (c_int, [P, P]),
     "sgb_fbp_sino_filter": (c_int, [P, c_int, c_ll, P, c_int, c_int, P, c_int, P]),
     "sgb_cbct_back": (c_int, [P, P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, c_float,

@@ -310,3 +310,16 @@ def test_ctpar_slices_equal_sinopar_fbp(cuda):
     for j in range(rg.nt - 1):  # the last row is dropped by the whole-tap rule 1 <= floor(bt) < nt
         close(vol[j], S.fbp(plan2, np.ascontiguousarray(proj[:, j, :])))
     assert np.all(vol[rg.nt - 1] == 0)
+
+
+def test_bounded_wait_expires_with_an_error_status(cuda):
+    """Failure detection without a GPU fault: a wait that nothing completes runs out of its
+    (1 ms) budget, the call returns SGB_ERR_TIMEOUT with the message, and the context keeps
+    working for the next reconstruction."""
+    from sinograms import _lib
+    st = _lib.lib().sgb_selftest_wait_timeout(2_000_000, None)
+    assert st == _lib.SGB_ERR_TIMEOUT
+    assert "bounded wait expired" in _lib.last_error()
+    f, c = fix("fdk_flat"), C.FDK_FLAT
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), window=S.Window(c["window"]))
+    close(S.fdk(plan, f["proj"]), f["ref"])
