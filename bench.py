@@ -79,6 +79,20 @@ def _peaks():
         return {}
 
 
+def _issue_roofline(updates, back_ms, clocks):
+    """The bound the back-projector actually meets: SM instruction issue.  Thread
+    instructions per update come from the committed ncu capture of this kernel at this
+    size; the peak is 152 SMs x 4 schedulers x 32 lanes per cycle at the sampled SM clock."""
+    ipu = _from_profile("fdk_tma_kernel_bench_issue.md", "thread_instructions_per_update")
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    peak = 152 * 4 * 32 * mhz * 1e6
+    if ipu is None:
+        return None
+    achieved = ipu * updates / (back_ms / 1e3)
+    return {"thread_instructions_per_update": ipu, "achieved_per_s": achieved, "peak_per_s": peak,
+            "frac": achieved / peak, "source": "profiles/fdk_tma_kernel_bench_issue.md (ncu smsp__inst_executed)"}
+
+
 def _filter_roofline(form, peaks):
     """Tensor-core work of the ramp filter (split-BF16 GEMM on first differences): 2 x rows x
     K x N x products, K = ns rounded up to 32, N = the output columns the MMAs compute
@@ -97,17 +111,21 @@ def _filter_roofline(form, peaks):
             "tensor_flops_per_launch": flops, "peak_source": "MEASURED_PEAKS.json bf16_tflops (burst)"}
 
 
-def _traffic_from_profile(name: str):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/<name>.md
-    (a line 'traffic_bytes_per_launch: N'), or None."""
+def _from_profile(name: str, key: str):
+    """A figure recorded from an ncu capture in profiles/<name> (a line 'key: N'), or None."""
     p = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(p):
-            if line.strip().startswith("traffic_bytes_per_launch:"):
+            if line.strip().startswith(key + ":"):
                 return float(line.split(":", 1)[1].split()[0])
     except Exception:
         pass
     return None
+
+
+def _traffic_from_profile(name: str):
+    """DRAM bytes per launch (line 'traffic_bytes_per_launch: N' of profiles/<name>)."""
+    return _from_profile(name, "traffic_bytes_per_launch")
 
 
 class ClockSampler:
@@ -253,6 +271,7 @@ def run_ours(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if hbm else "missing",
                      "alg_bytes_per_launch": alg_bytes,
                      "traffic": _traffic_from_profile("fdk_tma_kernel_bench_dram.md"),
+                     "issue": _issue_roofline(upd, f["back_ms"], f["clocks"]),
                      "fp32_issue": {"flops_per_update": F_UPD,
                                     "achieved_tflops": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12,
                                     "peak_tflops_nominal": NOMINAL_FP32_TFLOPS,
