@@ -50,7 +50,17 @@
 #include "sgb_kernels.cuh"
 #include "sgb_tc.cuh"
 
+#include <cooperative_groups.h>
+
 namespace sgb {
+
+int num_sms() {
+    static int n[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
+    return n[dev];
+}
 
 namespace {
 
@@ -64,6 +74,7 @@ constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kAPiece = kM * kKc * 2;  // bytes of one BF16 piece of the d tile
 constexpr int kBPiece = kN * kKc * 2;  // bytes of one BF16 piece of the H tile
 constexpr int kTmemCols = 2 * kN;
+constexpr int kPartStride = kN + 4;  // floats per row of a split-K partial (16-byte pad: no bank conflicts)
 
 template <int NP>
 struct Cfg {
@@ -73,6 +84,10 @@ struct Cfg {
     static constexpr int kBufs = NP == 3 ? 1 : 2;  // accumulator sets in the 512 TMEM columns
     static constexpr size_t kSmem = 1024 + (size_t)kStages * kStageBytes + 256;
 };
+
+static_assert((size_t)kM * kPartStride * 4 <= (size_t)Cfg<2>::kStages * Cfg<2>::kStageBytes &&
+                  (size_t)kM * kPartStride * 4 <= (size_t)Cfg<3>::kStages * Cfg<3>::kStageBytes,
+              "a split-K partial must fit in the idle pipeline ring");
 
 // piece pairs (p, q) with p + q < NP: d_p * H_q
 __device__ __forceinline__ int prod_a(int i) { return (0x012010 >> (4 * i)) & 0xF; }  // 0,1,0,2,1,0
@@ -225,10 +240,13 @@ __device__ __forceinline__ void store_row32<__nv_bfloat16>(__nv_bfloat16 *dst, c
     }
 }
 
+__device__ __forceinline__ void store_one(float *d, float v) { *d = v; }
+__device__ __forceinline__ void store_one(__nv_bfloat16 *d, float v) { *d = __float2bfloat16_rn(v); }
+
 template <int NP, typename TO>
 __global__ void __launch_bounds__(kThreads, 1)
     filter_gemm_kernel(const FilterArgs A, const __grid_constant__ CUtensorMap dmap,
-                       const __grid_constant__ CUtensorMap hmap) {
+                       const __grid_constant__ CUtensorMap hmap, int ksplit) {
     using C = Cfg<NP>;
     constexpr int NS = C::kStages;
     extern __shared__ uint8_t smem_raw[];
@@ -266,6 +284,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     const long long ntiles = (A.nrows + kM - 1) / kM * A.nblk;
     const int nk = A.kpad / kKc;
+    // Split-K (ksplit > 1): the grid is ntiles * ksplit CTAs in clusters of ksplit along x;
+    // cluster rank r runs K steps [kb, ke) of tile blockIdx.x / ksplit.  Otherwise persistent.
+    const int rank = (int)(blockIdx.x % (unsigned)ksplit);
+    const long long t_first = blockIdx.x / ksplit, t_step = gridDim.x / ksplit;
+    const int kchunk = (nk + ksplit - 1) / ksplit;
+    const int kb = rank * kchunk, ke = min(nk, kb + kchunk);
 
     if (warp == 0) {
         // ------------------------------------------------------------ TMA producer
@@ -274,10 +298,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&hmap)) : "memory");
             uint32_t it = 0;
             bool ok = true;
-            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+            for (long long tile = t_first; tile < ntiles && ok; tile += t_step) {
                 const int m0 = (int)(tile / A.nblk) * kM;
                 const int n0 = (int)(tile % A.nblk) * kN;
-                for (int kc = 0; kc < nk; kc++) {
+                for (int kc = kb; kc < ke; kc++) {
                     const int s = it % NS;
                     if (!lane_wait(empty + s, ((it / NS) & 1) ^ 1, abort_flag, A.err, 1)) {
                         ok = false;
@@ -309,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) {
             uint32_t it = 0, j = 0;
             bool ok = true;
-            for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, j++) {
+            for (long long tile = t_first; tile < ntiles && ok; tile += t_step, j++) {
                 const uint32_t buf = j % C::kBufs, use = j / C::kBufs;
                 if (!lane_wait(accempty + buf, (use & 1) ^ 1, abort_flag, A.err, 2)) {
                     ok = false;
@@ -321,7 +345,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t idesc = tc::idesc_bf16_f32(kM, neff);
                 // NP = 3: columns [0, 256) take d0*H0, [256, 512) the five small products
                 const uint32_t dmain = tbase + buf * kN, dsmall = tbase + (NP == 3 ? kN : buf * kN);
-                for (int kc = 0; kc < nk; kc++) {
+                for (int kc = kb; kc < ke; kc++) {
                     const int s = it % NS;
                     if (!lane_wait(full + s, (it / NS) & 1, abort_flag, A.err, 2)) {
                         ok = false;
@@ -336,7 +360,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                             const uint64_t ad = tc::sdesc_k_sw64(a0 + prod_a(pr) * kAPiece + kk * 32);
                             const uint64_t bd = tc::sdesc_k_sw64(b0 + prod_b(pr) * kBPiece + kk * 32);
                             const bool small = NP == 3 && pr > 0;
-                            const uint32_t first = (kc | kk) == 0 && (pr == 0 || (small && pr == 1));
+                            const uint32_t first = kc == kb && kk == 0 && (pr == 0 || (small && pr == 1));
                             tc::mma_bf16(small ? dsmall : dmain, ad, bd, idesc, !first);
                         }
                     tc::commit(empty + s);  // frees the stage once these MMAs have read it
@@ -362,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int c0 = ((warp - 2) >> 2) * kEpiCols;
         TO *out = static_cast<TO *>(A.out);
         uint32_t j = 0;
-        for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, j++) {
+        for (long long tile = t_first; tile < ntiles; tile += t_step, j++) {
             const uint32_t buf = j % C::kBufs, use = j / C::kBufs;
             if (!warp_wait(accfull + buf, use & 1, abort_flag, A.err, 8)) break;
             tc::fence_after_sync();
@@ -370,6 +394,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int n0 = (int)(tile % A.nblk) * kN;
             const int ncols = min(kN, A.nout - n0);
             TO *orow = out + row * A.nout + n0;
+            // split-K partial: row (32 q + lane) of the idle ring, kPartStride floats per row
+            float *prow = reinterpret_cast<float *>(smem) + (32 * q + lane) * kPartStride;
             const uint32_t taddr = tbase + buf * kN + ((uint32_t)(32 * q) << 16);
             for (int cc = c0; cc < c0 + kEpiCols && cc < ncols; cc += 32) {
                 float v[32];
@@ -381,7 +407,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                 } else {
                     tc::ld32(taddr + cc, v);
                 }
-                if (row < A.nrows) store_row32<TO>(orow + cc, v, ncols - cc, A.ovec);
+                if (ksplit > 1) {
+#pragma unroll
+                    for (int i = 0; i < 32; i += 4)
+                        *reinterpret_cast<float4 *>(prow + cc + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                } else if (row < A.nrows) {
+                    store_row32<TO>(orow + cc, v, ncols - cc, A.ovec);
+                }
             }
             tc::fence_before_sync();
             __syncwarp();
@@ -394,14 +426,36 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     tc::fence_after_sync();
     if (warp == 1) tc::tmem_dealloc(tbase, kTmemCols);
-}
-
-int num_sms() {
-    static int n[64] = {};
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
-    if (!n[dev]) cudaDeviceGetAttribute(&n[dev], cudaDevAttrMultiProcessorCount, dev);
-    return n[dev];
+    if (ksplit > 1) {
+        // Rank r sums rows [r0, r1) of the tile over the cluster's partials in rank order.
+        // Every CTA reaches both barriers (the waits above are bounded), so none can hang.
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        cl.sync();
+        const long long tile = t_first;
+        const int m0 = (int)(tile / A.nblk) * kM, n0 = (int)(tile % A.nblk) * kN;
+        const int ncols = min(kN, A.nout - n0), nc4 = (ncols + 3) >> 2;
+        const int r0 = rank * kM / ksplit, r1 = min((rank + 1) * kM / ksplit, (int)(A.nrows - m0 < kM ? A.nrows - m0 : kM));
+        TO *out = static_cast<TO *>(A.out);
+        for (int idx = threadIdx.x; idx < (r1 - r0) * nc4; idx += kThreads) {
+            const int r = r0 + idx / nc4, c = 4 * (idx % nc4);
+            const float *src = reinterpret_cast<const float *>(smem) + r * kPartStride + c;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int qr = 0; qr < ksplit; qr++) {
+                const float4 b = *reinterpret_cast<const float4 *>(cl.map_shared_rank(src, qr));
+                a.x += b.x;
+                a.y += b.y;
+                a.z += b.z;
+                a.w += b.w;
+            }
+            const float v[4] = {a.x, a.y, a.z, a.w};
+            TO *dst = out + (long long)(m0 + r) * A.nout + n0 + c;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+                if (c + i < ncols) store_one(dst + i, v[i]);
+        }
+        cl.sync();  // peers' partials stay in place until every rank has read them
+    }
 }
 
 template <int NP, typename TO>
@@ -417,8 +471,36 @@ int launch_np(const FilterArgs &A, __nv_bfloat16 *D, const CUtensorMap &dmap, co
     const size_t smem = Cfg<NP>::kSmem;
     SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long tiles = (A.nrows + kM - 1) / kM * A.nblk;
-    const unsigned grid = (unsigned)std::min<long long>(tiles, sms);
-    k<<<grid, kThreads, smem, st>>>(A, dmap, hmap);
+    // Few tiles (e.g. one 2D sinogram): split K over a cluster of up to 8 CTAs per tile, as many
+    // as the SMs hold, with every rank keeping >= 1 K step.
+    const int nk = A.kpad / kKc;
+    int ksplit = 1;
+    if (tiles * 2 <= sms) {
+        ksplit = (int)std::min<long long>(8, std::min<long long>(sms / tiles, nk));
+        while (ksplit > 1 && (ksplit - 1) * ((nk + ksplit - 1) / ksplit) >= nk) ksplit--;
+    }
+    if (ksplit == 1) {
+        const unsigned grid = (unsigned)std::min<long long>(tiles, sms);
+        k<<<grid, kThreads, smem, st>>>(A, dmap, hmap, 1);
+        return after_launch("filter_gemm_kernel");
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(tiles * ksplit));
+    cfg.blockDim = dim3(kThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ksplit;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k, A, dmap, hmap, ksplit);
+    if (e != cudaSuccess) {
+        set_error("filter_gemm_kernel: split-K launch failed: %s", cudaGetErrorString(e));
+        return SGB_ERR_CUDA;
+    }
     return after_launch("filter_gemm_kernel");
 }
 

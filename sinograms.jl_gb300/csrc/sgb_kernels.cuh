@@ -52,6 +52,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn();
 // ---------------------------------------------------- view geometry table
 // per used view v (view index a = v * ia_skip): (sin, cos) in FP32 from FP64 angles.
 int launch_view_trig(const double *betas_dev, int na, int ia_skip, float2 *trig, cudaStream_t st);
+// streaming multiprocessors of the current device (cached per device)
+int num_sms();
 
 // -------------------------------------------------- FDK back-projection
 struct FdkArgs {
