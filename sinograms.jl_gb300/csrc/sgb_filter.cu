@@ -469,7 +469,13 @@ int launch_np(const FilterArgs &A, __nv_bfloat16 *D, const CUtensorMap &dmap, co
     SGB_TRY(after_launch("split_rows_kernel"));
     auto k = filter_gemm_kernel<NP, TO>;
     const size_t smem = Cfg<NP>::kSmem;
-    SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static bool attr_done[64] = {};  // per device
+    int dev = 0;
+    SGB_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
     const long long tiles = (A.nrows + kM - 1) / kM * A.nblk;
     // Few tiles (e.g. one 2D sinogram): split K over a cluster of up to 8 CTAs per tile, as many
     // as the SMs hold, with every rank keeping >= 1 K step.
@@ -596,21 +602,26 @@ int launch_filter_rows(const FilterArgs &A0, const FilterOperator &F, DevBuf &sc
     const int align = out_bf16 ? 8 : 4;
     A.ovec = (A.nout % align == 0) && (reinterpret_cast<uintptr_t>(out) % 16 == 0);
     SGB_TRY(scratch.reserve(filter_scratch_bytes(F, A.nrows)));
-    PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
-    SGB_REQUIRE(fn, "cuTensorMapEncodeTiled is not available from the driver");
-    CUtensorMap dmap;
-    cuuint64_t dims[3] = {(cuuint64_t)F.kpad, (cuuint64_t)A.nrows, (cuuint64_t)F.np};
-    cuuint64_t strides[2] = {(cuuint64_t)F.kpad * 2, (cuuint64_t)F.kpad * 2 * (cuuint64_t)A.nrows};
-    cuuint32_t box[3] = {(cuuint32_t)kKc, (cuuint32_t)kM, 1};
-    cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = fn(&dmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, scratch.p, dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("filter: cuTensorMapEncodeTiled failed (%d) for the split rows: kpad=%d rows=%lld", (int)r, F.kpad,
-                  A.nrows);
-        return SGB_ERR_CUDA;
+    if (F.dmap_ptr != scratch.p || F.dmap_rows != A.nrows) {
+        PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+        SGB_REQUIRE(fn, "cuTensorMapEncodeTiled is not available from the driver");
+        cuuint64_t dims[3] = {(cuuint64_t)F.kpad, (cuuint64_t)A.nrows, (cuuint64_t)F.np};
+        cuuint64_t strides[2] = {(cuuint64_t)F.kpad * 2, (cuuint64_t)F.kpad * 2 * (cuuint64_t)A.nrows};
+        cuuint32_t box[3] = {(cuuint32_t)kKc, (cuuint32_t)kM, 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        F.dmap_ptr = nullptr;
+        CUresult r = fn(&F.dmap, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, scratch.p, dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            set_error("filter: cuTensorMapEncodeTiled failed (%d) for the split rows: kpad=%d rows=%lld", (int)r,
+                      F.kpad, A.nrows);
+            return SGB_ERR_CUDA;
+        }
+        F.dmap_ptr = scratch.p;
+        F.dmap_rows = A.nrows;
     }
+    const CUtensorMap &dmap = F.dmap;
     __nv_bfloat16 *D = scratch.as<__nv_bfloat16>();
     if (F.np == 3)
         return out_bf16 ? launch_np<3, __nv_bfloat16>(A, D, dmap, F.map, st) : launch_np<3, float>(A, D, dmap, F.map, st);

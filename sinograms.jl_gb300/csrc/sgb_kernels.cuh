@@ -34,6 +34,10 @@ struct FilterOperator {
     int ns = 0, np = 0, kpad = 0, nblk = 0;
     DevBuf buf, err;
     CUtensorMap map;
+    // tensor map of the split rows, reused while the scratch pointer and row count repeat
+    mutable CUtensorMap dmap{};
+    mutable const void *dmap_ptr = nullptr;
+    mutable long long dmap_rows = -1;
     ~FilterOperator();
     // g: real(ifft(Hk)) (length npad); outputs up to nout_max columns per row
     int build(const std::vector<double> &g, int ns, int nout_max, int np, cudaStream_t st);

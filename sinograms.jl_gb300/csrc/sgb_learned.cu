@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "sgb_common.cuh"
+#include "sgb_kernels.cuh"
 #include "sgb_tc.cuh"
 
 namespace sgb {
@@ -33,6 +34,21 @@ __host__ __device__ constexpr int cout_of(int l) { return l == kLayers - 1 ? 1 :
 __host__ __device__ constexpr int wcount(int l) { return cout_of(l) * cin_of(l) * kK; }
 
 __device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+// Inference GELU x Phi(x), with erf by Abramowitz & Stegun 7.1.26 (Hastings' rational form,
+// |error| <= 1.5e-7): Phi(-|x|) = 0.5 P(t) exp(-u^2), u = |x| / sqrt 2, t = 1 / (1 + 0.3275911 u),
+// and Phi(|x|) = 1 - Phi(-|x|).  Branch-free, one reciprocal and one exp2; it differs from the
+// training GELU (erff) by ~1e-7, far below the network's BF16 weight precision.
+__device__ __forceinline__ float gelu_infer(float x) {
+    const float u = fabsf(x) * 0.70710678118654752f;
+    float t, e;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(fmaf(0.3275911f, u, 1.f)));
+    // 0.5 * (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5)
+    const float hp =
+        t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.5307027145f, -0.7265760135f), 0.7107068705f), -0.142248368f), 0.127414796f);
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(-u * u * 1.4426950408889634f));
+    const float h = hp * e;  // Phi(-|x|)
+    return x * (x >= 0.f ? 1.f - h : h);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
     const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
     const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
@@ -234,7 +250,7 @@ __global__ void scale_copy(const float *__restrict__ a, float s, float *__restri
 // advanced by k positions (16 B), so one staged tile serves all nine taps.  The weights
 // are staged the same way, [tap][ch / 8][co][8].
 constexpr int kTM = 128, kTPos = kTM + 2 * kPad;
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 512;  // 16 warps: warp w reads TMEM lane quarter w % 4, channel group w / 4
 constexpr int kTcABytes = 2 * (kC / 8) * kTPos * 16;  // two pieces
 constexpr int kTcWBytes = kK * (kC / 8) * kC * 16;
 
@@ -243,22 +259,35 @@ __device__ __forceinline__ uint64_t sdesc_k_none(uint32_t saddr, uint32_t lbo, u
            ((uint64_t)1 << 46);
 }
 
-// one position's 32 channels, split hi/lo, into a channel-group-major activation buffer
-__device__ __forceinline__ void store_split_cg(uint8_t *A, int pos, const float (&v)[32]) {
+// channels 8 cg .. 8 cg + 7 of one position, split hi/lo, into their channel group
+__device__ __forceinline__ void store_split8(uint8_t *A, int cg, int pos, const float (&v)[8]) {
+    uint32_t h[4], l[4];
 #pragma unroll
-    for (int cg = 0; cg < kC / 8; cg++) {
-        uint32_t h[4], l[4];
-#pragma unroll
-        for (int j = 0; j < 4; j++) {
-            __nv_bfloat162 a = __floats2bfloat162_rn(v[cg * 8 + 2 * j], v[cg * 8 + 2 * j + 1]);
-            const float2 af = __bfloat1622float2(a);
-            __nv_bfloat162 b = __floats2bfloat162_rn(v[cg * 8 + 2 * j] - af.x, v[cg * 8 + 2 * j + 1] - af.y);
-            h[j] = *reinterpret_cast<uint32_t *>(&a);
-            l[j] = *reinterpret_cast<uint32_t *>(&b);
-        }
-        *reinterpret_cast<uint4 *>(A + (cg * kTPos + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<uint4 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    for (int j = 0; j < 4; j++) {
+        __nv_bfloat162 a = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        const float2 af = __bfloat1622float2(a);
+        __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * j] - af.x, v[2 * j + 1] - af.y);
+        h[j] = *reinterpret_cast<uint32_t *>(&a);
+        l[j] = *reinterpret_cast<uint32_t *>(&b);
     }
+    *reinterpret_cast<uint4 *>(A + (cg * kTPos + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// channels 4 c4 .. 4 c4 + 3 of one position (half of channel group c4 / 2), split hi/lo
+__device__ __forceinline__ void store_split4(uint8_t *A, int c4, int pos, const float (&v)[4]) {
+    uint32_t h[2], l[2];
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        __nv_bfloat162 a = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        const float2 af = __bfloat1622float2(a);
+        __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * j] - af.x, v[2 * j + 1] - af.y);
+        h[j] = *reinterpret_cast<uint32_t *>(&a);
+        l[j] = *reinterpret_cast<uint32_t *>(&b);
+    }
+    const int cg = c4 >> 1, half = (c4 & 1) * 8;
+    *reinterpret_cast<uint2 *>(A + (cg * kTPos + pos) * 16 + half) = make_uint2(h[0], h[1]);
+    *reinterpret_cast<uint2 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16 + half) = make_uint2(l[0], l[1]);
 }
 
 // where each layer's BF16 weights and FP32 bias start in the parameter arrays
@@ -286,7 +315,7 @@ constexpr int kFZ = kTPos + 2 * kPad;  // z window: t in [ts - 20, ts + 124)
 constexpr size_t kFusedSmem = 3 * (size_t)kTcWBytes + 2 * (size_t)kTcABytes +
                               sizeof(float) * (2 * kC * kK + 4 * kC + 1 + kFZ) + 64;
 
-__global__ void __launch_bounds__(kTcThreads) lf_tc_fused(const float *__restrict__ z, float s,
+__global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__restrict__ z, float s,
                                                           const __nv_bfloat16 *__restrict__ wb, LayerWeights lw,
                                                           const __nv_bfloat16 *__restrict__ wp,
                                                           const float *__restrict__ p, float *__restrict__ y,
@@ -337,39 +366,45 @@ __global__ void __launch_bounds__(kTcThreads) lf_tc_fused(const float *__restric
             zw[j] = (t >= 0 && t < L) ? zr[t] : 0.f;
         }
         __syncthreads();
-        // layer 0 (1 -> 32, GELU) on all 136 window positions, into buffer 0
-        for (int pp = tid; pp < kTPos; pp += kTcThreads) {
+        // layer 0 (1 -> 32, GELU) on all 136 window positions, into buffer 0: one item per
+        // (position, 4 output channels), half a 16-byte channel-group row
+        for (int idx = tid; idx < kTPos * (kC / 4); idx += kTcThreads) {
+            const int pp = idx >> 3, c4 = idx & 7;
             const int t = ts - 16 + pp;
-            float v[kC];
+            float v[4];
 #pragma unroll
-            for (int co = 0; co < kC; co++) {
+            for (int j = 0; j < 4; j++) {
+                const int co = c4 * 4 + j;
                 float acc = bias[co];
 #pragma unroll
                 for (int k = 0; k < kK; k++) acc = fmaf(w0[co * kK + k], zw[pp + k] * inv_s, acc);
-                v[co] = (t >= 0 && t < L) ? gelu(acc) : 0.f;
+                v[j] = (t >= 0 && t < L) ? gelu_infer(acc) : 0.f;
             }
-            store_split_cg(Ab, pp, v);
+            store_split4(Ab, c4, pp, v);
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
         int cur = 0;
         for (int l = 0; l < 3 && ok; l++, cur ^= 1) {
+            int good = 1;
             if (tid == 0) {
                 tc::fence_after_sync();
+                // descriptors advance by start address only (bits 0-13 hold address / 16)
+                const uint64_t a0 = sdesc_k_none(ab0 + cur * kTcABytes, kTPos * 16, 128);
+                const uint64_t b0 = sdesc_k_none(wl0 + l * kTcWBytes, kC * 16, 128);
                 int n = 0;
+#pragma unroll
                 for (int piece = 0; piece < 2; piece++)
+#pragma unroll
                     for (int k = 0; k < kK; k++)
+#pragma unroll
                         for (int ks = 0; ks < kC / 16; ks++, n++) {
-                            const uint64_t ad = sdesc_k_none(
-                                ab0 + cur * kTcABytes + ((piece * (kC / 8) + 2 * ks) * kTPos + k) * 16, kTPos * 16, 128);
-                            const uint64_t bd =
-                                sdesc_k_none(wl0 + l * kTcWBytes + ((k * (kC / 8) + 2 * ks) * kC) * 16, kC * 16, 128);
+                            const uint64_t ad = a0 + (uint64_t)((piece * (kC / 8) + 2 * ks) * kTPos + k);
+                            const uint64_t bd = b0 + (uint64_t)((k * (kC / 8) + 2 * ks) * kC);
                             tc::mma_bf16(tbase, ad, bd, idesc, n != 0);
                         }
                 tc::commit(bar);
-            }
-            int good = 1;
-            if (lane == 0) {
+                // the issuing thread alone waits; the CTA barrier below releases the others
                 const long long c0 = clock64();
                 while (!dev::mbar_try_wait(bar, phase & 1))
                     if (clock64() - c0 > dev::kWaitBudget) {
@@ -378,18 +413,19 @@ __global__ void __launch_bounds__(kTcThreads) lf_tc_fused(const float *__restric
                         break;
                     }
             }
-            good = __shfl_sync(0xffffffffu, good, 0);
+            good = __syncthreads_and(good);
             phase++;
             tc::fence_after_sync();
             if (good) {
-                float v[32];
-                tc::ld32(tbase + ((uint32_t)(32 * warp) << 16), v);
-                const int pp = 4 + 32 * warp + lane;  // output row m = pp - 4
+                const int q = warp & 3, cg = warp >> 2;
+                float v[8];
+                tc::ld8(tbase + ((uint32_t)(32 * q) << 16) + 8 * cg, v);
+                const int pp = 4 + 32 * q + lane;  // output row m = pp - 4
                 const int t = ts - 16 + pp;
-                const float *bl = bias + (l + 1) * kC;
+                const float *bl = bias + (l + 1) * kC + 8 * cg;
 #pragma unroll
-                for (int co = 0; co < kC; co++) v[co] = (t >= 0 && t < L) ? gelu(v[co] + bl[co]) : 0.f;
-                store_split_cg(Ab + (cur ^ 1) * kTcABytes, pp, v);
+                for (int j = 0; j < 8; j++) v[j] = (t >= 0 && t < L) ? gelu_infer(v[j] + bl[j]) : 0.f;
+                store_split8(Ab + (cur ^ 1) * kTcABytes, cg, pp, v);
             }
             if (!__syncthreads_and(good)) ok = false;  // also orders the TMEM reads before the next MMAs
             tc::fence_proxy_async_smem();
@@ -398,30 +434,31 @@ __global__ void __launch_bounds__(kTcThreads) lf_tc_fused(const float *__restric
         }
         if (!ok) break;
         // last layer (32 -> 1) and the residual on the 104 exact positions
-        if (tid < kFOut) {
-            const int pp = 16 + tid, t = ts + tid;
-            if (t < L) {
-                const uint8_t *A = Ab + cur * kTcABytes;
-                float acc = bias[4 * kC];
+        // four threads per output position, one channel group each, summed by shuffles
+        // (threads < 416 fill warps 0-12 completely)
+        if (tid < kFOut * (kC / 8)) {
+            const int o = tid >> 2, cg = tid & 3;
+            const int pp = 16 + o, t = ts + o;
+            const uint8_t *A = Ab + cur * kTcABytes;
+            float pa[4] = {0.f, 0.f, 0.f, 0.f};  // one chain per channel pair j
 #pragma unroll
-                for (int k = 0; k < kK; k++) {
-                    const int row = pp - 4 + k;
+            for (int k = 0; k < kK; k++) {
+                const int row = pp - 4 + k;
+                const uint4 h = *reinterpret_cast<const uint4 *>(A + (cg * kTPos + row) * 16);
+                const uint4 q = *reinterpret_cast<const uint4 *>(A + ((kC / 8 + cg) * kTPos + row) * 16);
+                const uint32_t hv[4] = {h.x, h.y, h.z, h.w}, qv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-                    for (int cg = 0; cg < kC / 8; cg++) {
-                        const uint4 h = *reinterpret_cast<const uint4 *>(A + (cg * kTPos + row) * 16);
-                        const uint4 q = *reinterpret_cast<const uint4 *>(A + ((kC / 8 + cg) * kTPos + row) * 16);
-                        const uint32_t hv[4] = {h.x, h.y, h.z, h.w}, qv[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-                        for (int j = 0; j < 4; j++) {
-                            const float a0 = __uint_as_float(hv[j] << 16) + __uint_as_float(qv[j] << 16);
-                            const float a1 = __uint_as_float(hv[j] & 0xFFFF0000u) + __uint_as_float(qv[j] & 0xFFFF0000u);
-                            acc = fmaf(w4[(cg * 8 + 2 * j) * kK + k], a0, acc);
-                            acc = fmaf(w4[(cg * 8 + 2 * j + 1) * kK + k], a1, acc);
-                        }
-                    }
+                for (int j = 0; j < 4; j++) {
+                    const float a0 = __uint_as_float(hv[j] << 16) + __uint_as_float(qv[j] << 16);
+                    const float a1 = __uint_as_float(hv[j] & 0xFFFF0000u) + __uint_as_float(qv[j] & 0xFFFF0000u);
+                    pa[j] = fmaf(w4[(cg * 8 + 2 * j) * kK + k], a0, pa[j]);
+                    pa[j] = fmaf(w4[(cg * 8 + 2 * j + 1) * kK + k], a1, pa[j]);
                 }
-                y[r * L + t] = zw[pp + 4] + s * acc;
             }
+            float acc = (pa[0] + pa[1]) + (pa[2] + pa[3]);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+            acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+            if (cg == 0 && t < L) y[r * L + t] = zw[pp + 4] + s * (bias[4 * kC] + acc);
         }
         __syncthreads();
     }
@@ -555,10 +592,14 @@ int lf_forward_tc(sgb_lf *F, const float *zdev, long long R, int L, float *ydev,
         lw.bias[l] = F->off.b[l];
     }
     const long long ntiles = R * ((L + kFOut - 1) / kFOut);
-    int dev = 0, sms = 0;
+    int dev = 0;
     SGB_CUDA(cudaGetDevice(&dev));
-    SGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    SGB_CUDA(cudaFuncSetAttribute(lf_tc_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem));
+    const int sms = num_sms();
+    static bool attr_done[64] = {};  // per device
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        SGB_CUDA(cudaFuncSetAttribute(lf_tc_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFusedSmem));
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
     const unsigned grid = (unsigned)std::min<long long>(ntiles, 2ll * sms);
     lf_tc_fused<<<grid, kTcThreads, kFusedSmem, st>>>(zdev, F->scale, wb, lw, wp, p, ydev, R, L, F->terr.as<int>());
     return after_launch("lf_tc_fused");

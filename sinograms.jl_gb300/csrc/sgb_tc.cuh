@@ -92,6 +92,19 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// 8 consecutive FP32 columns of this thread's TMEM lane, waited like ld32.
+__device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
+}
+
 // Two 32-column blocks (e.g. the two accumulators of one output block) with one wait.
 __device__ __forceinline__ void ld32x2(uint32_t ta, uint32_t tb, float (&va)[32], float (&vb)[32]) {
     uint32_t a[32], b[32];
