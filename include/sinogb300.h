@@ -16,7 +16,11 @@
  * are device pointers on the current CUDA device.  Geometry vectors (angles, sin/cos
  * tables, pixel-centre axes, filter responses) are always small host arrays.
  * `stream` is a cudaStream_t (NULL = legacy default stream).  Calls block until the
- * result is complete unless flags has SGB_ASYNC (device pointers only).
+ * result is complete unless flags has SGB_ASYNC: with device pointers for every call, and
+ * with host pointers for the plan calls (sgb_fdk, sgb_fbp, sgb_fbp_filter_rows,
+ * sgb_fbp_backproject), whose copies then run on `stream` from and into the caller's
+ * buffers -- keep them valid (and page-locked, for copies that overlap other work) until
+ * the stream is synchronised.  sgb_plan_sync waits and reports the plan's device errors.
  */
 #ifndef SINOGB300_H
 #define SINOGB300_H
@@ -232,6 +236,9 @@ SGB_API int sgb_fbp_filter_rows(sgb_plan *plan, const float *sino, float *filter
 SGB_API int sgb_fbp_backproject(sgb_plan *plan, const float *filtered, float *image, int nslices,
                                 int flags, void *stream);
 SGB_API int sgb_plan_destroy(sgb_plan *plan);
+/* Waits for `stream` and returns the error status of the plan's last asynchronous calls
+ * (the device flags that a synchronous fdk/fbp call checks before returning). */
+SGB_API int sgb_plan_sync(sgb_plan *plan, void *stream);
 /* Stage timing (no counterpart in the reference): when enabled, fdk/fbp record CUDA
  * events on the call's stream around the filter and back-projection kernels;
  * sgb_plan_last_timing waits for them and returns ms[0] = weighted filter,

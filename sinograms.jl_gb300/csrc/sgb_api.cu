@@ -117,9 +117,11 @@ int filter_status(int e) {
 }
 
 // finish() plus, for synchronous calls, the filter's error word
+// Plan calls keep their host staging buffers in the plan, so SGB_ASYNC also holds for host
+// pointers: the call returns with its copies and kernels enqueued (sgb_plan_sync reports).
 int plan_done(sgb_plan *P, int flags, cudaStream_t st) {
+    if (flags & SGB_ASYNC) return SGB_OK;
     SGB_TRY(finish(flags, st));
-    if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
     int e = 0;
     SGB_CUDA(cudaMemcpy(&e, P->filt_err, sizeof(int), cudaMemcpyDeviceToHost));
     return filter_status(e);
@@ -442,6 +444,20 @@ int sgb_plan_destroy(sgb_plan *plan) {
     return SGB_OK;
 }
 
+int sgb_plan_sync(sgb_plan *P, void *stream) {
+    SGB_REQUIRE(P, "plan_sync: null plan");
+    cudaStream_t st = as_stream(stream);
+    SGB_CUDA(cudaStreamSynchronize(st));
+    if (!P->flags.p) return SGB_OK;
+    int f[4] = {0, 0, 0, 0};
+    SGB_CUDA(cudaMemcpy(f, P->flags.p, sizeof f, cudaMemcpyDeviceToHost));
+    if (f[2]) {
+        set_error("fdk: back-projector reported error flags 0x%x (1: box undersized, 2/4: wait timeout)", f[2]);
+        return (f[2] & 6) ? SGB_ERR_TIMEOUT : SGB_ERR_CUDA;
+    }
+    return filter_status(f[3]);
+}
+
 int sgb_plan_info(const sgb_plan *P, int *info, int n) {
     SGB_REQUIRE(P && info && n >= 5, "plan_info: bad argument");
     info[0] = P->tma ? 1 : 0;
@@ -521,8 +537,8 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
         P->mark(2, st);
         if (!(flags & SGB_DEVICE_PTRS))
             SGB_CUDA(cudaMemcpyAsync(image, img_dev, nvox * sizeof(float), cudaMemcpyDeviceToHost, st));
+        if (flags & SGB_ASYNC) return SGB_OK;
         SGB_TRY(finish(flags, st));
-        if ((flags & SGB_ASYNC) && (flags & SGB_DEVICE_PTRS)) return SGB_OK;
         int err[2] = {0, 0};
         SGB_CUDA(cudaMemcpy(err, P->flags.as<int>() + 2, sizeof err, cudaMemcpyDeviceToHost));
         if (err[0]) {
@@ -664,6 +680,7 @@ int sgb_fbp_backproject(sgb_plan *P, const float *filtered, float *image, int ns
     SGB_TRY(launch_back2(A, st));
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(image, img_dev, npix * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (flags & SGB_ASYNC) return SGB_OK;
     return finish(flags, st);
 }
 

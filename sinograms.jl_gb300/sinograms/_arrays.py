@@ -52,6 +52,15 @@ def stream_for(device: bool):
     return None
 
 
+def plan_call(device: bool, sync: bool):
+    """(flags, stream) of a plan call: with sync=False host buffers are also copied
+    asynchronously, on torch's current stream (keep them alive, and pinned, until
+    plan.sync())."""
+    flags = (_lib.SGB_DEVICE_PTRS if device else 0) | (0 if sync else _lib.SGB_ASYNC)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream) if (device or not sync) else None
+    return flags, st
+
+
 def empty(shape, like: Arr, dtype=np.float32):
     if like.device:
         return torch.empty(shape, dtype=torch.float32, device=like.obj.device)

@@ -10,7 +10,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._arrays import Arr, empty, f64, flags_for, ptr, stream_for
+from ._arrays import Arr, empty, f64, flags_for, plan_call, ptr, stream_for, torch
 from .filters import SinogramsArgumentError, Window, fbp_filter, fdk_view_weight, fbp_view_weight
 from .geom import CtFan, ImageGeom, SinoPar, _ar, _dso, _rfov, c_struct, dims, is_ct
 
@@ -77,6 +77,11 @@ class _Plan:
         _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 5), "plan_info")
         return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]))
 
+    def sync(self):
+        """Wait for torch's current stream and raise the device errors of asynchronous calls."""
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _status(_lib.lib().sgb_plan_sync(self._h, st), "plan_sync")
+
     def last_timing(self):
         """(filter_ms, back_ms) of the last fdk/fbp call (needs set_timing)."""
         ms = np.zeros(2)
@@ -120,13 +125,15 @@ def plan_fbp(rg, ig: ImageGeom, window: Window = Window(), npad: int | None = No
 
 def fdk(plan: FDKplan, proj, out=None, sync: bool = True):
     """image = fdk(plan, proj), fdk.jl:65-81.  proj in numpy order (na, nt, ns) ->
-    image (nz, ny, nx).  CUDA tensors stay on the device."""
+    image (nz, ny, nx).  CUDA tensors stay on the device.  With sync=False the call only
+    enqueues its work on torch's current stream, host copies included (plan.sync() waits)."""
     rg = plan.rg
     a = Arr(proj)
     if tuple(reversed(a.shape)) != dims(rg):
         raise SinogramsArgumentError(f"size mismatch {tuple(reversed(a.shape))} {dims(rg)}")  # fdk.jl:68-69
     img = out if out is not None else empty(tuple(reversed(plan.ig.dims)), a)
-    _status(_lib.lib().sgb_fdk(plan.handle, a.ptr, ptr(img), flags_for(a.device, sync), stream_for(a.device)), "fdk")
+    flags, st = plan_call(a.device, sync)
+    _status(_lib.lib().sgb_fdk(plan.handle, a.ptr, ptr(img), flags, st), "fdk")
     return img
 
 
@@ -139,8 +146,8 @@ def _fbp_plan(plan: FBPNormalPlan, sino, out=None, sync=True):
     nsl = int(np.prod(shp[2:])) if len(shp) > 2 else 1
     oshape = tuple(reversed(plan.ig.dims)) if len(shp) == 2 else tuple(a.shape[:-2]) + tuple(reversed(plan.ig.dims))
     img = out if out is not None else empty(oshape, a)
-    _status(_lib.lib().sgb_fbp(plan.handle, a.ptr, ptr(img), nsl, flags_for(a.device, sync), stream_for(a.device)),
-            "fbp")
+    flags, st = plan_call(a.device, sync)
+    _status(_lib.lib().sgb_fbp(plan.handle, a.ptr, ptr(img), nsl, flags, st), "fbp")
     return img
 
 

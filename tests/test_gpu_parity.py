@@ -323,3 +323,31 @@ def test_bounded_wait_expires_with_an_error_status(cuda):
     f, c = fix("fdk_flat"), C.FDK_FLAT
     plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), window=S.Window(c["window"]))
     close(S.fdk(plan, f["proj"]), f["ref"])
+
+
+def test_async_host_plan_calls_match_blocking(cuda):
+    """fdk / fbp with host buffers and sync=False enqueue the copies and kernels on the
+    current stream; after plan.sync() the result equals the blocking call's."""
+    import torch
+    rng = np.random.default_rng(7)
+    rg = S.CtFanFlat(ns=64, nt=32, ds=1.0, dt=1.0, dsd=500.0, dod=200.0, na=48)
+    plan = S.plan_fbp(rg, S.ImageGeom((32, 32, 16), (1.0, 1.0, 1.0)))
+    proj = rng.standard_normal((48, 32, 64)).astype(np.float32)
+    ref = S.fdk(plan, proj)
+    hp = torch.from_numpy(proj).pin_memory()
+    out = torch.empty(ref.shape, dtype=torch.float32, pin_memory=True)
+    st = torch.cuda.Stream()
+    with torch.cuda.stream(st):
+        S.fdk(plan, hp.numpy(), out=out.numpy(), sync=False)
+        plan.sync()
+    assert np.array_equal(out.numpy(), ref)
+    rg2 = S.SinoFanFlat(nb=96, d=1.0, na=60, orbit=360.0, dsd=400.0, dod=150.0)
+    plan2 = S.plan_fbp(rg2, S.ImageGeom((48, 48), (1.5, 1.5)))
+    sino = rng.standard_normal((60, 96)).astype(np.float32)
+    ref2 = S.fbp(plan2, sino)
+    hs = torch.from_numpy(sino).pin_memory()
+    out2 = torch.empty(ref2.shape, dtype=torch.float32, pin_memory=True)
+    with torch.cuda.stream(st):
+        S.fbp(plan2, hs.numpy(), out=out2.numpy(), sync=False)
+        plan2.sync()
+    assert np.array_equal(out2.numpy(), ref2)
