@@ -299,6 +299,8 @@ def run_ours(args):
     }
     if not args.no_batch:
         line["batched"] = measure_batched(args)
+    if not args.no_2d:
+        line["configs_2d"] = measure_2d(args)
     if ws == 1 and rank == 0 and not args.no_cpu:
         base, acc = cpu_leg({k: v.cpu().numpy() for k, v in outs.items()}, proj.cpu().numpy())
         line["cpu_baseline"] = base
@@ -345,6 +347,89 @@ def measure_batched(args):
             "work_items": info["work_items"], "persistent_ctas": info["ctas"], "persistent_launches": info["launches"],
             "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps,
             "stage_ms": {"filters": stages[0], "back_by_box_class": stages[1:]}}
+
+
+def _per_call_ms(fn, reps):
+    """Device time per call of fn (enqueued back to back on the current stream)."""
+    import torch
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measure_2d(args):
+    """The 2D workloads beside the headline, device-resident, on seeded synthetic inputs:
+    SinoPar 256 x 180 -> 256^2 with a Hann window; SinoFanArc 888 x 512 views over a short scan ->
+    512^2 (Parker weights, 0.5% noise); and the learned row filter's sparse-view scan (888 x 90
+    views over 360 deg -> 512^2, flat detector): plain against learned FBP time, and image RMSE
+    against the phantom on 8 held-out scans."""
+    import torch
+
+    import sinograms as S
+    from sinograms import learned as LF
+    reps = max(args.steps, 20)
+    out = {}
+    try:
+        rg = S.SinoPar(nb=256, d=1.0, na=180, orbit=180.0)
+        plan = S.plan_fbp(rg, S.ImageGeom((256, 256), (1.0, 1.0)), window=S.Window("hann"))
+        sino = S.ellipse_sino(rg, S.random_ellipses(10, 1, 100.0), device=True)
+        ms = _per_call_ms(lambda: S.fbp(plan, sino, sync=False), reps)
+        plan.set_timing(True)
+        S.fbp(plan, sino)
+        f_ms, b_ms = plan.last_timing()
+        plan.set_timing(False)
+        out["par_256x180_hann"] = {"ms_per_fbp": ms, "filter_ms": f_ms, "back_ms": b_ms,
+                                   "back_updates_per_s": 256 * 256 * 180 / (b_ms / 1e3)}
+        base = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=2, orbit=360.0)
+        orbit = 180.0 + 2.0 * float(np.degrees(S._gamma_max(base)))  # short scan: 180 deg + fan angle
+        rg = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=512, orbit=orbit)
+        plan = S.plan_fbp(rg, S.ImageGeom((512, 512), (0.9766, 0.9766)))
+        sino = S.ellipse_sino(rg, S.random_ellipses(20, 2, 220.0, axes=(4.0, 120.0), dens=(-0.3, 1.0)), device=True)
+        g = torch.Generator(device="cuda").manual_seed(102)
+        sino = sino + 0.005 * sino.abs().max() * torch.randn(sino.shape, device="cuda", generator=g)
+        ms = _per_call_ms(lambda: S.fbp(plan, sino, sync=False), reps)
+        plan.set_timing(True)
+        S.fbp(plan, sino)
+        f_ms, b_ms = plan.last_timing()
+        plan.set_timing(False)
+        out["arc_888x512_short_scan"] = {"ms_per_fbp": ms, "filter_ms": f_ms, "back_ms": b_ms,
+                                         "back_updates_per_s": 512 * 512 * 512 / (b_ms / 1e3)}
+        rg, ig = LF.sparse_fan_geometry()
+        plan = S.plan_fbp(rg, ig)
+        lf = LF.LearnedFilter.load(LF.default_weights_path())
+        geo = S.BddGeo.from_geoms(rg, ig)
+        mask = torch.as_tensor(ig.mask, device="cuda")
+        gen = torch.Generator(device="cuda").manual_seed(900000)
+        rp, rl, kept = [], [], 0
+        for i in range(8):
+            img = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000 + i))
+            s = LF.dd_project(img, geo)
+            s = s + 0.005 * s.abs().max() * torch.randn(s.shape, device="cuda", generator=gen)
+            rp.append(float((S.fbp(plan, s) - img)[mask].pow(2).mean().sqrt()))
+            im_l, info = LF.fbp_learned(plan, lf, s, judge=True)
+            rl.append(float((LF.fbp_backproject(plan, lf.apply(LF.fbp_filter_rows(plan, s))) - img)[mask]
+                            .pow(2).mean().sqrt()))
+            kept += int(info["used"] == "learned")
+        s = s.contiguous()
+        ms_plain = _per_call_ms(lambda: S.fbp(plan, s, sync=False), reps)
+        ms_learned = _per_call_ms(lambda: LF.fbp_backproject(
+            plan, lf.apply(LF.fbp_filter_rows(plan, s, sync=False), sync=False), sync=False), reps)
+        z = LF.fbp_filter_rows(plan, s)
+        ms_net = _per_call_ms(lambda: lf.apply(z, sync=False), reps)
+        out["learned_filter_flat_888x90"] = {
+            "ms_plain_fbp": ms_plain, "ms_learned_fbp": ms_learned, "ms_network": ms_net,
+            "rmse_vs_phantom_plain": float(np.mean(rp)), "rmse_vs_phantom_learned": float(np.mean(rl)),
+            "judge_kept_learned": f"{kept}/8", "weights": os.path.basename(LF.default_weights_path())}
+    except Exception as e:  # the headline line must still print
+        out["error"] = f"{type(e).__name__}: {e}"
+    return out
 
 
 # --------------------------------------------------------------------- CPU side
@@ -523,6 +608,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
+    ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
     ap.add_argument("--case", choices=["fdk-180v", "fdk-batch"], help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
     args = ap.parse_args()
