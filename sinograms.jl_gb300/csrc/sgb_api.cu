@@ -256,11 +256,13 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
 }
 
 // Filtered-projection layout and back-projector choice for an FDK plan: rows padded to
-// a multiple of 8 samples (16-byte TMA strides for both storage types); the TMA-staged
-// kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.
+// a multiple of 8 samples (16-byte TMA strides for every storage type); the TMA-staged
+// kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.  FP32 storage
+// for the TMA-staged kernel holds pairs (y, y[next] - y), 8 bytes per sample; the direct
+// kernel reads plain FP32 samples.
 int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool tune) {
     const sgb_ct_geom &g = P->cg;
-    const int elem = P->storage == SGB_STORE_BF16 ? 2 : 4;
+    const int elem = P->storage == SGB_STORE_BF16 ? 2 : 8;
     P->pitch = (g.ns + 7) / 8 * 8;
     SGB_TRY(P->filt_buf.reserve((size_t)P->pitch * g.nt * g.na * elem));
     SGB_CUDA(cudaMemsetAsync(P->filt_buf.p, 0, (size_t)P->pitch * g.nt * g.na * elem, st));
@@ -295,7 +297,14 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     double rx = std::fabs(ig->deltas[0]) * (ig->dims[0] / 2.0 + std::fabs(ig->offsets[0]) + 1);
     double ry = std::fabs(ig->deltas[1]) * (ig->dims[1] / 2.0 + std::fabs(ig->offsets[1]) + 1);
     P->tma = false;
-    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) SGB_TRY(fdk_tma_autotune(P, st, tune));
+    if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) {
+        SGB_TRY(fdk_tma_autotune(P, st, tune));
+        if (!P->tma && A.elem_bytes == 8) {  // pair boxes too large: plain FP32 boxes
+            A.elem_bytes = 4;
+            SGB_TRY(fdk_tma_autotune(P, st, tune));
+        }
+    }
+    if (!P->tma && A.elem_bytes == 8) A.elem_bytes = 4;  // direct kernel: plain FP32 rows
     return SGB_OK;
 }
 
@@ -506,8 +515,10 @@ static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *o
     A.sBt = P->sBt;
     A.scale = P->scale;
     A.err = P->filt_err;
-    return launch_filter_rows(A, P->filt, P->split_shared ? *P->split_shared : P->split, out,
-                              P->storage == SGB_STORE_BF16, st);
+    const int kind = P->storage == SGB_STORE_BF16 ? FILTER_OUT_BF16
+                                                  : (P->ct && P->tma && P->targs.elem_bytes == 8 ? FILTER_OUT_PAIR
+                                                                                                 : FILTER_OUT_F32);
+    return launch_filter_rows(A, P->filt, P->split_shared ? *P->split_shared : P->split, out, kind, st);
 }
 
 int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *stream) {
@@ -902,7 +913,7 @@ struct sgb_batch {
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t ev[6] = {};  // graph event nodes: start, filters done, each class done
+    cudaEvent_t ev[8] = {};  // graph event nodes: start, filters done, each class done
     ~sgb_batch() {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
@@ -963,36 +974,39 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     SGB_CUDA(cudaGetDevice(&dev));
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::vector<size_t> class_begin;
-    for (int W : {32, 64, 128}) {
-        std::vector<int> order;
-        int box_bytes = 0;
-        for (int i = 0; i < n; i++)
-            if (scans[i].W == W) {
-                order.push_back(i);
-                box_bytes = std::max(box_bytes, scans[i].box_bytes);
+    for (int ecls : {8, 4, 2}) {  // element size: FP32 pairs, FP32, BF16
+        for (int W : {32, 64, 128}) {
+            std::vector<int> order;
+            int box_bytes = 0;
+            for (int i = 0; i < n; i++)
+                if (scans[i].W == W && scans[i].elem_bytes == ecls) {
+                    order.push_back(i);
+                    box_bytes = std::max(box_bytes, scans[i].box_bytes);
+                }
+            if (order.empty()) continue;
+            elem = ecls;
+            std::sort(order.begin(), order.end(), [&](int a, int b) { return scans[a].nv > scans[b].nv; });
+            FdkBatchArgs C{};
+            C.nscans = n;
+            C.W = W;
+            C.box_bytes = box_bytes;
+            C.elem_bytes = elem;
+            C.vps = 4;
+            if (fdk_batch_smem(C) > 200 * 1024) C.vps = 2;
+            if (fdk_batch_smem(C) > 200 * 1024) C.vps = 1;
+            SGB_REQUIRE(fdk_batch_smem(C) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
+            class_begin.push_back(work.size());
+            for (int i : order) {
+                const FdkTmaArgs &A = scans[i];
+                const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
+                for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
             }
-        if (order.empty()) continue;
-        std::sort(order.begin(), order.end(), [&](int a, int b) { return scans[a].nv > scans[b].nv; });
-        FdkBatchArgs C{};
-        C.nscans = n;
-        C.W = W;
-        C.box_bytes = box_bytes;
-        C.elem_bytes = elem;
-        C.vps = 4;
-        if (fdk_batch_smem(C) > 200 * 1024) C.vps = 2;
-        if (fdk_batch_smem(C) > 200 * 1024) C.vps = 1;
-        SGB_REQUIRE(fdk_batch_smem(C) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
-        class_begin.push_back(work.size());
-        for (int i : order) {
-            const FdkTmaArgs &A = scans[i];
-            const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
-            for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
+            C.nwork = (int)(work.size() - class_begin.back());
+            B->classes.push_back(C);
         }
-        C.nwork = (int)(work.size() - class_begin.back());
-        B->classes.push_back(C);
     }
     SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
-    SGB_REQUIRE(B->classes.size() <= 4, "batch_fdk: too many box classes");
+    SGB_REQUIRE(B->classes.size() <= 6, "batch_fdk: too many box classes");
     for (size_t c = 0; c < B->classes.size(); c++) {
         FdkBatchArgs &C = B->classes[c];
         C.scans = B->scans.as<FdkTmaArgs>();

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kThreads)
                     mbar_arrive_expect_tx(full + st, (uint32_t)(nvalid * W * A.H * (int)sizeof(TP)));
                     for (int v = 0; v < nvalid; v++) {
                         const int2 o = origin[st * VPS + v];
-                        tma_load_3d(stage_base + (size_t)(st * VPS + v) * box_bytes, &maps.m[wk.x], o.x, o.y,
+                        tma_load_3d(stage_base + (size_t)(st * VPS + v) * box_bytes, &maps.m[wk.x], o.x * kXS<TP>, o.y,
                                     (g * VPS + v) * A.ia_skip, full + st);
                     }
                 }
@@ -212,6 +212,9 @@ size_t fdk_batch_smem(const FdkBatchArgs &B) {
 }
 
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B) {
+    if (B.elem_bytes == 8)
+        return B.W == 32 ? batch_occupancy<float2, 32>(B)
+                         : (B.W == 64 ? batch_occupancy<float2, 64>(B) : batch_occupancy<float2, 128>(B));
     if (B.elem_bytes == 4)
         return B.W == 32 ? batch_occupancy<float, 32>(B)
                          : (B.W == 64 ? batch_occupancy<float, 64>(B) : batch_occupancy<float, 128>(B));
@@ -220,6 +223,10 @@ int fdk_batch_ctas_per_sm(const FdkBatchArgs &B) {
 }
 
 int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
+    if (B.elem_bytes == 8)
+        return B.W == 32 ? launch_batch_t<float2, 16, 32>(B, maps, nctas, st)
+                         : (B.W == 64 ? launch_batch_t<float2, 16, 64>(B, maps, nctas, st)
+                                      : launch_batch_t<float2, 16, 128>(B, maps, nctas, st));
     if (B.elem_bytes == 4)
         return B.W == 32 ? launch_batch_t<float, 16, 32>(B, maps, nctas, st)
                          : (B.W == 64 ? launch_batch_t<float, 16, 64>(B, maps, nctas, st)

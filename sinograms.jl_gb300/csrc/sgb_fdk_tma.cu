@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kThreads)
                 mbar_arrive_expect_tx(full + st, (uint32_t)(nvalid * W * H * (int)sizeof(TP)));
                 for (int v = 0; v < nvalid; v++) {
                     const int2 o = origin[st * VPS + v];
-                    tma_load_3d(stage_base + (size_t)(st * VPS + v) * box_bytes, &map, o.x, o.y,
+                    tma_load_3d(stage_base + (size_t)(st * VPS + v) * box_bytes, &map, o.x * kXS<TP>, o.y,
                                 (g * VPS + v) * A.ia_skip, full + st);
                 }
             }
@@ -204,8 +204,9 @@ size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage) {
 }
 
 int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st) {
-    // exhaustive box extent over all tiles and views (same device arithmetic as the kernel)
-    A.align = A.elem_bytes == 4 ? 4 : 8;
+    // exhaustive box extent over all tiles and views (same device arithmetic as the kernel);
+    // box origins aligned so the TMA x coordinate is a multiple of 16 bytes
+    A.align = A.elem_bytes == 2 ? 8 : 4;
     const int ntx = floor_div_up(A.nx, kTX), nty = floor_div_up(A.ny, kTY), ntz = floor_div_up(A.nz, A.zu);
     SGB_CUDA(cudaMemsetAsync(ext_dev, 0, 2 * sizeof(int), st));
     const long long n = (long long)ntx * nty * ntz * A.nv;
@@ -229,11 +230,17 @@ int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st) {
 
 bool fdk_tma_choose(FdkTmaArgs &A) {
     if (A.W > 128 || A.H <= 1 || A.H > 256) return false;
-    if (fdk_tma_smem(A, 4, kNStage) <= 200 * 1024) A.vps = 4;
-    else if (fdk_tma_smem(A, 2, kNStage) <= 200 * 1024) A.vps = 2;
-    else if (fdk_tma_smem(A, 1, kNStage) <= 200 * 1024) A.vps = 1;
-    else return false;
-    return encode_fn() != nullptr;
+    // most views per stage that still lets two CTAs share an SM, else the most that fit
+    A.vps = 0;
+    for (int budget : {112 * 1024, 200 * 1024}) {
+        for (int v : {4, 2, 1})
+            if (fdk_tma_smem(A, v, kNStage) <= (size_t)budget) {
+                A.vps = v;
+                break;
+            }
+        if (A.vps) break;
+    }
+    return A.vps && encode_fn() != nullptr;
 }
 
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map) {
@@ -242,11 +249,13 @@ int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap
         set_error("cuTensorMapEncodeTiled is not available from the driver");
         return SGB_ERR_CUDA;
     }
-    cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)A.nt, (cuuint64_t)A.na};
+    // pair rows (elem_bytes 8) are described as FP32 rows of twice the length
+    const int xs = A.elem_bytes == 8 ? 2 : 1;
+    cuuint64_t dims[3] = {(cuuint64_t)pitch * xs, (cuuint64_t)A.nt, (cuuint64_t)A.na};
     cuuint64_t strides[2] = {(cuuint64_t)pitch * A.elem_bytes, (cuuint64_t)pitch * A.nt * A.elem_bytes};
-    cuuint32_t box[3] = {(cuuint32_t)A.W, (cuuint32_t)A.H, 1};
+    cuuint32_t box[3] = {(cuuint32_t)(A.W * xs), (cuuint32_t)A.H, 1};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = fn(map, A.elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3,
+    CUresult r = fn(map, A.elem_bytes == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                     const_cast<void *>(filt), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -257,6 +266,10 @@ int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap
 }
 
 int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+    if (A.elem_bytes == 8) {
+        if (A.is_arc) return A.zu == 16 ? launch_t<float2, true, 16>(A, map, st) : launch_t<float2, true, 32>(A, map, st);
+        return A.zu == 16 ? launch_t<float2, false, 16>(A, map, st) : launch_t<float2, false, 32>(A, map, st);
+    }
     if (A.elem_bytes == 4) {
         if (A.is_arc) return A.zu == 16 ? launch_t<float, true, 16>(A, map, st) : launch_t<float, true, 32>(A, map, st);
         return A.zu == 16 ? launch_t<float, false, 16>(A, map, st) : launch_t<float, false, 32>(A, map, st);

@@ -17,6 +17,8 @@ constexpr int kTX = 16, kTY = 16;             // columns per CTA
 constexpr int kConsumers = kTX * kTY;          // 8 consumer warps
 constexpr int kThreads = kConsumers + 32;      // + 1 producer warp
 constexpr int kNStage = 4;                     // stages in the ring (views per stage: 4, 2 or 1)
+// TMA x coordinate per box sample: pair boxes (y, dy) are two FP32 elements per sample
+template <typename TP> constexpr int kXS = sizeof(TP) == 8 ? 2 : 1;
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
 
@@ -102,6 +104,22 @@ __device__ __forceinline__ float lds(const __nv_bfloat16 *, uint32_t a) {
     return __uint_as_float((uint32_t)h << 16);
 }
 
+// A row's s-interpolation at box address a: fs between samples c and c+1 (cbct-back.jl:205).
+// FP32 and BF16 boxes hold samples (two loads); pair boxes hold (y[c], y[c+1] - y[c]) written by
+// the filter, one 8-byte load and the same arithmetic fma(fs, y[c+1] - y[c], y[c]).
+template <typename TP>
+__device__ __forceinline__ float srow(uint32_t a, float fs) {
+    if constexpr (sizeof(TP) == 8) {
+        float v, d;
+        asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v), "=f"(d) : "r"(a));
+        return fmaf(fs, d, v);
+    } else {
+        const TP *tag = nullptr;
+        const float p0 = lds(tag, a), p1 = lds(tag, a + (uint32_t)sizeof(TP));
+        return fmaf(fs, p1 - p0, p0);
+    }
+}
+
 // (a != b) ? x : y as one compare and one select, never a branch.
 __device__ __forceinline__ float sel_ne(uint32_t a, uint32_t b, float x, float y) {
     float d;
@@ -168,18 +186,14 @@ __device__ __forceinline__ ColView view_setup(const FdkTmaArgs &A, float x, floa
 
 template <typename TP, int ZU, int W>
 __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) {
-    constexpr uint32_t RB = W * sizeof(TP), SZ = sizeof(TP);  // bytes per box row / sample
-    const TP *tag = nullptr;
+    constexpr uint32_t RB = W * sizeof(TP);  // bytes per box row
     if (g.mode == 1) {
         // magic_floor's bits are it + 0x4B400000: fold that offset into the base address
         const uint32_t kb = g.sb - 0x4B400000u * RB;
         float m = __fadd_rd(g.bt0, 12582912.0f);
         uint32_t bits = __float_as_uint(m), a = kb + bits * RB;
-        float p0 = lds(tag, a), p1 = lds(tag, a + SZ);
-        float lo_v = fmaf(g.fs, p1 - p0, p0);  // :205
-        p0 = lds(tag, a + RB);
-        p1 = lds(tag, a + RB + SZ);
-        float hi_v = fmaf(g.fs, p1 - p0, p0);  // :206
+        float lo_v = srow<TP>(a, g.fs);       // :205
+        float hi_v = srow<TP>(a + RB, g.fs);  // :206
         acc[0] = fmaf(g.w2, fmaf(g.bt0 - (m - 12582912.0f), hi_v - lo_v, lo_v), acc[0]);  // :208
         uint32_t prev = bits;
 #pragma unroll
@@ -188,8 +202,7 @@ __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) 
             m = __fadd_rd(bt, 12582912.0f);
             bits = __float_as_uint(m);
             a = kb + RB + bits * RB;  // upper row it+1
-            const float q0 = lds(tag, a), q1 = lds(tag, a + SZ);
-            const float nv = fmaf(g.fs, q1 - q0, q0);
+            const float nv = srow<TP>(a, g.fs);
             lo_v = sel_ne(bits, prev, hi_v, lo_v);  // advanced one row: the old upper row
             hi_v = nv;
             prev = bits;
@@ -203,10 +216,8 @@ __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) 
             const float m = __fadd_rd(bt, 12582912.0f);
             const uint32_t a = kb + __float_as_uint(m) * RB;
             const float ft = bt - (m - 12582912.0f);
-            const float p00 = lds(tag, a), p10 = lds(tag, a + SZ);
-            const float p01 = lds(tag, a + RB), p11 = lds(tag, a + RB + SZ);
-            const float a0 = fmaf(g.fs, p10 - p00, p00);
-            const float a1 = fmaf(g.fs, p11 - p01, p01);
+            const float a0 = srow<TP>(a, g.fs);
+            const float a1 = srow<TP>(a + RB, g.fs);
             acc[k] = fmaf(g.w2, fmaf(ft, a1 - a0, a0), acc[k]);
         }
     } else if (g.mode == 3) {
@@ -220,10 +231,8 @@ __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) 
             const uint32_t a = g.sb + (uint32_t)((ok ? it : g.lo) * (int)RB);  // dropped taps read a safe row
             const float wk = ok ? g.w2 : 0.f;
             const float ft = bt - fit;
-            const float p00 = lds(tag, a), p10 = lds(tag, a + SZ);
-            const float p01 = lds(tag, a + RB), p11 = lds(tag, a + RB + SZ);
-            const float a0 = fmaf(g.fs, p10 - p00, p00);           // :205
-            const float a1 = fmaf(g.fs, p11 - p01, p01);           // :206
+            const float a0 = srow<TP>(a, g.fs);                    // :205
+            const float a1 = srow<TP>(a + RB, g.fs);               // :206
             acc[k] = fmaf(wk, fmaf(ft, a1 - a0, a0), acc[k]);       // :208
         }
     }

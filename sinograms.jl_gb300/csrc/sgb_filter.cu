@@ -43,6 +43,7 @@
 // flag, the MMA issuer drains its MMAs, the producer waits (bounded) for its copies in
 // flight, and tensor memory is freed before the CTA exits.
 #include <cstring>
+#include <type_traits>
 
 #include <cuda_bf16.h>
 
@@ -243,6 +244,41 @@ __device__ __forceinline__ void store_row32<__nv_bfloat16>(__nv_bfloat16 *dst, c
 __device__ __forceinline__ void store_one(float *d, float v) { *d = v; }
 __device__ __forceinline__ void store_one(__nv_bfloat16 *d, float v) { *d = __float2bfloat16_rn(v); }
 
+// FP32 pair output (y[i], y[i+1] - y[i]): the element type of FILTER_OUT_PAIR rows.
+struct PairOut {};
+template <typename TO> struct OutElem { using T = TO; };
+template <> struct OutElem<PairOut> { using T = float2; };
+
+// Pairs of 32 columns of a row: v[i] with the difference to the next column (v[i+1], or
+// `next` for i = 31); `last` is the first column with no successor in the row (difference 0).
+__device__ __forceinline__ void store_pairs32(float2 *dst, const float (&v)[32], float next, int n, int last,
+                                              bool vec) {
+    float d[32];
+#pragma unroll
+    for (int i = 0; i < 32; i++) d[i] = i >= last ? 0.f : (i < 31 ? v[i + 1] : next) - v[i];
+    if (vec && n >= 32) {
+#pragma unroll
+        for (int i = 0; i < 32; i += 2)
+            *reinterpret_cast<float4 *>(dst + i) = make_float4(v[i], d[i], v[i + 1], d[i + 1]);
+    } else {
+#pragma unroll
+        for (int i = 0; i < 32; i++)
+            if (i < n) dst[i] = make_float2(v[i], d[i]);
+    }
+}
+
+// Pair differences across output tiles: column b = kN j - 1 of every row takes y[b+1] - y[b]
+// once both tiles are written.
+__global__ void pair_seam_kernel(float2 *__restrict__ out, long long nrows, int nout, int nblk) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (nblk < 2 || i >= nrows * (nblk - 1)) return;
+    const long long row = i / (nblk - 1);
+    const int b = (1 + (int)(i % (nblk - 1))) * kN - 1;
+    if (b + 1 >= nout) return;
+    float2 *r = out + row * nout;
+    r[b].y = r[b + 1].x - r[b].x;
+}
+
 template <int NP, typename TO>
 __global__ void __launch_bounds__(kThreads, 1)
     filter_gemm_kernel(const FilterArgs A, const __grid_constant__ CUtensorMap dmap,
@@ -384,7 +420,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int q = warp & 3;                              // TMEM lane quarter this warp may read
         constexpr int kEpiCols = kN / (kEpiWarps / 4);       // columns per epilogue warp
         const int c0 = ((warp - 2) >> 2) * kEpiCols;
-        TO *out = static_cast<TO *>(A.out);
+        using TE = typename OutElem<TO>::T;
+        TE *out = static_cast<TE *>(A.out);
         uint32_t j = 0;
         for (long long tile = t_first; tile < ntiles; tile += t_step, j++) {
             const uint32_t buf = j % C::kBufs, use = j / C::kBufs;
@@ -393,7 +430,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             const long long row = tile / A.nblk * kM + 32 * q + lane;
             const int n0 = (int)(tile % A.nblk) * kN;
             const int ncols = min(kN, A.nout - n0);
-            TO *orow = out + row * A.nout + n0;
+            TE *orow = out + row * A.nout + n0;
             // split-K partial: row (32 q + lane) of the idle ring, kPartStride floats per row
             float *prow = reinterpret_cast<float *>(smem) + (32 * q + lane) * kPartStride;
             const uint32_t taddr = tbase + buf * kN + ((uint32_t)(32 * q) << 16);
@@ -411,6 +448,20 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
                     for (int i = 0; i < 32; i += 4)
                         *reinterpret_cast<float4 *>(prow + cc + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+                } else if constexpr (std::is_same<TO, PairOut>::value) {
+                    // successor of the chunk's last column: from TMEM inside the tile (warp-uniform
+                    // condition), else a row end (0) or the next tile (pair_seam_kernel)
+                    float next = 0.f;
+                    if (cc + 32 < kN && cc + 32 < ncols) {
+                        if (NP == 3) {
+                            float a, b;
+                            tc::ld1x2(taddr + cc + 32, taddr + kN + cc + 32, &a, &b);
+                            next = a + b;
+                        } else {
+                            next = tc::ld1(taddr + cc + 32);
+                        }
+                    }
+                    if (row < A.nrows) store_pairs32(orow + cc, v, next, ncols - cc, A.nout - 1 - (n0 + cc), A.ovec);
                 } else if (row < A.nrows) {
                     store_row32<TO>(orow + cc, v, ncols - cc, A.ovec);
                 }
@@ -436,26 +487,48 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int m0 = (int)(tile / A.nblk) * kM, n0 = (int)(tile % A.nblk) * kN;
         const int ncols = min(kN, A.nout - n0), nc4 = (ncols + 3) >> 2;
         const int r0 = rank * kM / ksplit, r1 = min((rank + 1) * kM / ksplit, (int)(A.nrows - m0 < kM ? A.nrows - m0 : kM));
-        TO *out = static_cast<TO *>(A.out);
+        using TE = typename OutElem<TO>::T;
+        TE *out = static_cast<TE *>(A.out);
         for (int idx = threadIdx.x; idx < (r1 - r0) * nc4; idx += kThreads) {
             const int r = r0 + idx / nc4, c = 4 * (idx % nc4);
             const float *src = reinterpret_cast<const float *>(smem) + r * kPartStride + c;
             float4 a = make_float4(0.f, 0.f, 0.f, 0.f);
+            float nx = 0.f;  // column c + 4, for the pair form
+            const bool has_next = std::is_same<TO, PairOut>::value && c + 4 < ncols && c + 4 < kN;
             for (int qr = 0; qr < ksplit; qr++) {
-                const float4 b = *reinterpret_cast<const float4 *>(cl.map_shared_rank(src, qr));
+                const float *ps = cl.map_shared_rank(src, qr);
+                const float4 b = *reinterpret_cast<const float4 *>(ps);
                 a.x += b.x;
                 a.y += b.y;
                 a.z += b.z;
                 a.w += b.w;
+                if (has_next) nx += ps[4];
             }
             const float v[4] = {a.x, a.y, a.z, a.w};
-            TO *dst = out + (long long)(m0 + r) * A.nout + n0 + c;
+            TE *dst = out + (long long)(m0 + r) * A.nout + n0 + c;
 #pragma unroll
-            for (int i = 0; i < 4; i++)
-                if (c + i < ncols) store_one(dst + i, v[i]);
+            for (int i = 0; i < 4; i++) {
+                if (c + i >= ncols) continue;
+                if constexpr (std::is_same<TO, PairOut>::value) {
+                    const int col = n0 + c + i;
+                    const float d = col + 1 >= A.nout ? 0.f : (i < 3 ? v[i + 1] : nx) - v[i];
+                    dst[i] = make_float2(v[i], d);
+                } else {
+                    store_one(dst + i, v[i]);
+                }
+            }
         }
         cl.sync();  // peers' partials stay in place until every rank has read them
     }
+}
+
+template <typename TO>
+int launch_seam(const FilterArgs &A, cudaStream_t st) {
+    if (!std::is_same<TO, PairOut>::value || A.nblk < 2) return SGB_OK;
+    const long long n = A.nrows * (A.nblk - 1);
+    pair_seam_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(static_cast<float2 *>(A.out), A.nrows, A.nout,
+                                                                  A.nblk);
+    return after_launch("pair_seam_kernel");
 }
 
 template <int NP, typename TO>
@@ -488,7 +561,8 @@ int launch_np(const FilterArgs &A, __nv_bfloat16 *D, const CUtensorMap &dmap, co
     if (ksplit == 1) {
         const unsigned grid = (unsigned)std::min<long long>(tiles, sms);
         k<<<grid, kThreads, smem, st>>>(A, dmap, hmap, 1);
-        return after_launch("filter_gemm_kernel");
+        SGB_TRY(after_launch("filter_gemm_kernel"));
+        return launch_seam<TO>(A, st);
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(tiles * ksplit));
@@ -507,7 +581,8 @@ int launch_np(const FilterArgs &A, __nv_bfloat16 *D, const CUtensorMap &dmap, co
         set_error("filter_gemm_kernel: split-K launch failed: %s", cudaGetErrorString(e));
         return SGB_ERR_CUDA;
     }
-    return after_launch("filter_gemm_kernel");
+    SGB_TRY(after_launch("filter_gemm_kernel"));
+    return launch_seam<TO>(A, st);
 }
 
 uint16_t bf16_bits(float f) {
@@ -587,7 +662,7 @@ size_t filter_scratch_bytes(const FilterOperator &F, long long nrows) {
     return (size_t)F.np * (size_t)nrows * F.kpad * sizeof(uint16_t);
 }
 
-int launch_filter_rows(const FilterArgs &A0, const FilterOperator &F, DevBuf &scratch, void *out, int out_bf16,
+int launch_filter_rows(const FilterArgs &A0, const FilterOperator &F, DevBuf &scratch, void *out, int out_kind,
                        cudaStream_t st) {
     if (A0.nrows <= 0) return SGB_OK;
     SGB_REQUIRE(A0.ns == F.ns, "filter: operator built for ns=%d, rows have %d samples", F.ns, A0.ns);
@@ -599,7 +674,8 @@ int launch_filter_rows(const FilterArgs &A0, const FilterOperator &F, DevBuf &sc
     A.kpad = F.kpad;
     A.nblk = (A.nout + kN - 1) / kN;
     A.err = A0.err ? A0.err : F.err.as<int>();
-    const int align = out_bf16 ? 8 : 4;
+    SGB_REQUIRE(out_kind >= FILTER_OUT_F32 && out_kind <= FILTER_OUT_PAIR, "filter: bad output form %d", out_kind);
+    const int align = out_kind == FILTER_OUT_BF16 ? 8 : (out_kind == FILTER_OUT_PAIR ? 2 : 4);
     A.ovec = (A.nout % align == 0) && (reinterpret_cast<uintptr_t>(out) % 16 == 0);
     SGB_TRY(scratch.reserve(filter_scratch_bytes(F, A.nrows)));
     if (F.dmap_ptr != scratch.p || F.dmap_rows != A.nrows) {
@@ -623,9 +699,14 @@ int launch_filter_rows(const FilterArgs &A0, const FilterOperator &F, DevBuf &sc
     }
     const CUtensorMap &dmap = F.dmap;
     __nv_bfloat16 *D = scratch.as<__nv_bfloat16>();
-    if (F.np == 3)
-        return out_bf16 ? launch_np<3, __nv_bfloat16>(A, D, dmap, F.map, st) : launch_np<3, float>(A, D, dmap, F.map, st);
-    return out_bf16 ? launch_np<2, __nv_bfloat16>(A, D, dmap, F.map, st) : launch_np<2, float>(A, D, dmap, F.map, st);
+    if (F.np == 3) {
+        if (out_kind == FILTER_OUT_PAIR) return launch_np<3, PairOut>(A, D, dmap, F.map, st);
+        return out_kind == FILTER_OUT_BF16 ? launch_np<3, __nv_bfloat16>(A, D, dmap, F.map, st)
+                                           : launch_np<3, float>(A, D, dmap, F.map, st);
+    }
+    if (out_kind == FILTER_OUT_PAIR) return launch_np<2, PairOut>(A, D, dmap, F.map, st);
+    return out_kind == FILTER_OUT_BF16 ? launch_np<2, __nv_bfloat16>(A, D, dmap, F.map, st)
+                                       : launch_np<2, float>(A, D, dmap, F.map, st);
 }
 
 }  // namespace sgb

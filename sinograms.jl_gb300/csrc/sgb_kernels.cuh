@@ -44,10 +44,14 @@ struct FilterOperator {
     // reads back (and reports) the kernel's error flags; synchronises st
     int check(cudaStream_t st);
 };
+// Output forms of launch_filter_rows: FP32 rows, BF16 rows, or FP32 pairs (y[i], y[i+1] - y[i])
+// -- the FDK back-projector's layout, one 8-byte shared load per s-interpolation.  A pair's
+// difference at a row's last column is 0.
+enum { FILTER_OUT_F32 = 0, FILTER_OUT_BF16 = 1, FILTER_OUT_PAIR = 2 };
 // Weighted, differenced, split rows go through `scratch` (grown to filter_scratch_bytes;
 // pre-size it before stream capture).
 size_t filter_scratch_bytes(const FilterOperator &F, long long nrows);
-int launch_filter_rows(const FilterArgs &A, const FilterOperator &F, DevBuf &scratch, void *out, int out_bf16,
+int launch_filter_rows(const FilterArgs &A, const FilterOperator &F, DevBuf &scratch, void *out, int out_kind,
                        cudaStream_t st);
 
 // cuTensorMapEncodeTiled from the driver entry-point table (null when unavailable)

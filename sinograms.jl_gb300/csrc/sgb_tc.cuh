@@ -92,6 +92,30 @@ __device__ __forceinline__ void ld32(uint32_t taddr, float (&v)[32]) {
     for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
 }
 
+// One FP32 column of this thread's TMEM lane (and one of each of two accumulators).
+__device__ __forceinline__ float ld1(uint32_t taddr) {
+    uint32_t r;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r)
+        : "r"(taddr)
+        : "memory");
+    return __uint_as_float(r);
+}
+__device__ __forceinline__ void ld1x2(uint32_t ta, uint32_t tb, float *a, float *b) {
+    uint32_t r, q;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%2];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x1.b32 {%1}, [%3];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r), "=r"(q)
+        : "r"(ta), "r"(tb)
+        : "memory");
+    *a = __uint_as_float(r);
+    *b = __uint_as_float(q);
+}
+
 // 8 consecutive FP32 columns of this thread's TMEM lane, waited like ld32.
 __device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
     uint32_t r[8];
