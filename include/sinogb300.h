@@ -247,7 +247,8 @@ SGB_API int sgb_plan_set_timing(sgb_plan *plan, int enable);
 SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
 /* Execution layout of a plan (no counterpart in the reference): info[0] = 1 when FDK
  * back-projection uses the TMA-staged kernel, info[1..2] = staged box (samples),
- * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z. */
+ * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z,
+ * info[5] (when n >= 6) = launches the views are split over. */
 SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
 
 /* ------------------------------------------------------- learned filter */

@@ -195,16 +195,17 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
     memset(&key, 0, sizeof key);
     key = TuneKey{g.kind, g.ns, g.nt, g.na, P->nx, P->ny, P->nz, A.elem_bytes, (float)g.dsd, (float)(g.dsd - g.dod),
                   (float)g.ds, (float)g.dt, A.dx, A.dy, A.dz};
-    int best_zu = 0;
+    // a candidate is (voxels per thread along z, launches the views are split over), coded zu * 4 + passes
+    int best = 0;
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         auto it = g_tune_cache.find(key);
-        if (it != g_tune_cache.end()) best_zu = it->second;
+        if (it != g_tune_cache.end()) best = it->second;
     }
     const long long updates = (long long)P->nx * P->ny * P->nz * g.na;
-    const int candidates[2] = {16, 32};
-    if (!tune) best_zu = 16;
-    if (!best_zu) {
+    const int candidates[4] = {16 * 4 + 1, 32 * 4 + 1, 16 * 4 + 2, 32 * 4 + 2};
+    if (!tune) best = 16 * 4 + 1;
+    if (!best) {
         float best_ms = 1e30f;
         cudaEvent_t e0, e1;
         SGB_CUDA(cudaEventCreate(&e0));
@@ -212,13 +213,14 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
         DevBuf img;
         const bool time_it = updates > (1ll << 30);  // small problems: take the default
         if (time_it) SGB_TRY(img.reserve((size_t)P->nx * P->ny * P->nz * sizeof(float)));
-        for (int zu : candidates) {
+        for (int cand : candidates) {
             FdkTmaArgs T = A;
-            T.zu = zu;
+            T.zu = cand / 4;
+            T.passes = cand % 4;
             SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
             if (!fdk_tma_choose(T)) continue;
             if (!time_it) {
-                best_zu = zu;
+                best = cand;
                 break;
             }
             CUtensorMap map;
@@ -234,19 +236,20 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
             SGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
             if (ms < best_ms) {
                 best_ms = ms;
-                best_zu = zu;
+                best = cand;
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
-        if (best_zu) {
+        if (best) {
             std::lock_guard<std::mutex> lock(g_tune_mu);
-            g_tune_cache[key] = best_zu;
+            g_tune_cache[key] = best;
         }
     }
-    if (!best_zu) return SGB_OK;  // the direct kernel handles this geometry
-    A.zu = best_zu;
+    if (!best) return SGB_OK;  // the direct kernel handles this geometry
+    A.zu = best / 4;
+    A.passes = best % 4;
     SGB_TRY(fdk_tma_prepare(A, P->flags.as<int>(), st));
     if (!fdk_tma_choose(A)) return SGB_OK;
     SGB_TRY(fdk_tma_encode(A, P->filt_buf.p, P->pitch, &P->tmap));
@@ -291,6 +294,9 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     A.dz = (float)(ig->deltas[2] / g.ds);
     A.is_arc = g.kind == SGB_ARC;
     A.zu = 16;
+    A.v0 = 0;
+    A.accum = 0;
+    A.passes = 1;
     A.elem_bytes = elem;
     A.err = P->flags.as<int>() + 2;
     // voxels must stay well inside the source circle for the corner bound to hold
@@ -474,6 +480,7 @@ int sgb_plan_info(const sgb_plan *P, int *info, int n) {
     info[2] = P->targs.H;
     info[3] = P->pitch;
     info[4] = P->targs.zu;
+    if (n >= 6) info[5] = P->targs.passes;
     return SGB_OK;
 }
 
@@ -960,6 +967,9 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     for (int i = 0; i < n; i++) {
         sgb_plan *P = B->plans[i];
         FdkTmaArgs A = P->targs;
+        A.v0 = 0;  // the batched kernel runs every view of a scan in one pass
+        A.accum = 0;
+        A.passes = 1;
         A.image = P->img_buf.as<float>();
         A.mask = P->mask_dev;
         A.err = B->flags.as<int>();

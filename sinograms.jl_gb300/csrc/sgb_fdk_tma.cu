@@ -95,8 +95,8 @@ __global__ void __launch_bounds__(kThreads)
                 float2 sc = make_float2(0.f, 1.f);
                 float zs = 0.f;
                 if (v < A.nv) {
-                    sc = A.trig[v];
-                    if (A.zsrc) zs = A.zsrc[v];
+                    sc = A.trig[A.v0 + v];
+                    if (A.zsrc) zs = A.zsrc[A.v0 + v];
                     int s0, t0, w, h;
                     tile_box<ARC>(A, sc.x, sc.y, xlo, xhi, ylo, yhi, zlo - zs, zhi - zs, &s0, &t0, &w, &h);
                     o = make_int2(s0, t0);
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kThreads)
                 for (int v = 0; v < nvalid; v++) {
                     const int2 o = origin[st * VPS + v];
                     tma_load_3d(stage_base + (size_t)(st * VPS + v) * box_bytes, &map, o.x * kXS<TP>, o.y,
-                                (g * VPS + v) * A.ia_skip, full + st);
+                                (A.v0 + g * VPS + v) * A.ia_skip, full + st);
                 }
             }
             issued = g + 1;
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kThreads)
         const int iz = iz0 + k;
         if (iz >= A.nz) break;
         const long long idx = ix + (long long)A.nx * (iy + (long long)A.ny * iz);
-        float v = acc[k];
+        float v = A.accum ? A.image[idx] + acc[k] : acc[k];
         if (A.mask && !A.mask[idx]) v = 0.f;  // :133
         A.image[idx] = v;
     }
@@ -265,7 +265,7 @@ int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap
     return SGB_OK;
 }
 
-int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+int launch_fdk_tma_views(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
     if (A.elem_bytes == 8) {
         if (A.is_arc) return A.zu == 16 ? launch_t<float2, true, 16>(A, map, st) : launch_t<float2, true, 32>(A, map, st);
         return A.zu == 16 ? launch_t<float2, false, 16>(A, map, st) : launch_t<float2, false, 32>(A, map, st);
@@ -279,6 +279,20 @@ int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st)
                           : launch_t<__nv_bfloat16, true, 32>(A, map, st);
     return A.zu == 16 ? launch_t<__nv_bfloat16, false, 16>(A, map, st)
                       : launch_t<__nv_bfloat16, false, 32>(A, map, st);
+}
+
+// All views, in A.passes launches over consecutive view ranges (the later ones accumulate):
+// a pass's working set in L2 is its views' share of each z-slab's detector rows.
+int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+    const int passes = std::max(1, std::min(A.passes, A.nv));
+    for (int p = 0; p < passes; p++) {
+        FdkTmaArgs T = A;
+        T.v0 = A.v0 + (int)((long long)A.nv * p / passes);
+        T.nv = (int)((long long)A.nv * (p + 1) / passes) - (T.v0 - A.v0);
+        T.accum = A.accum || p > 0;
+        SGB_TRY(launch_fdk_tma_views(T, map, st));
+    }
+    return SGB_OK;
 }
 
 }  // namespace sgb

@@ -21,6 +21,9 @@ struct FdkTmaArgs {
     int align;              // TMA x-coordinate alignment in elements
     int W, H, box_bytes;    // staged box (samples) and its shared-memory footprint
     int vps;                // views per pipeline stage (4, or 2 for large boxes)
+    int v0;                 // first view of this launch (views v0 .. v0 + nv - 1)
+    int accum;              // 1: add to the volume (a later pass over views), 0: overwrite
+    int passes;             // launches the views are split over (chosen by the plan's autotuner)
 };
 
 // Batched persistent back-projection: per-scan arguments in device memory, tensor maps in

@@ -73,9 +73,9 @@ class _Plan:
 
     def info(self) -> dict:
         """Execution layout: TMA-staged FDK kernel in use, staged box, row pitch, z-unroll."""
-        a = np.zeros(5, dtype=np.int32)
-        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 5), "plan_info")
-        return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]))
+        a = np.zeros(6, dtype=np.int32)
+        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 6), "plan_info")
+        return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]), view_passes=int(a[5]))
 
     def sync(self):
         """Wait for torch's current stream and raise the device errors of asynchronous calls."""
