@@ -55,5 +55,10 @@ size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage);
 // 3D tensor map over the filtered projections (pitch, nt, na).
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map);
 int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+// one storage form each (sgb_fdk_tma_<form>.cu)
+int launch_fdk_tma_pair_flat(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+int launch_fdk_tma_pair_arc(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+int launch_fdk_tma_f32(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+int launch_fdk_tma_bf16(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
 
 }  // namespace sgb

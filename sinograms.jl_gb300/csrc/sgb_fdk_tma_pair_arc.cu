@@ -1,0 +1,10 @@
+// sgb_fdk_tma_pair_arc.cu -- TMA-staged FDK back-projection instantiated for FP32 pairs (y, y[next] - y), arc detector.
+#include "sgb_fdk_tma_kernel.cuh"
+
+namespace sgb {
+
+int launch_fdk_tma_pair_arc(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+    return fdkdev::launch_form<float2, true>(A, map, st);
+}
+
+}  // namespace sgb
