@@ -204,7 +204,10 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
     }
     const long long updates = (long long)P->nx * P->ny * P->nz * g.na;
     std::vector<int> candidates = {16 * 4 + 1, 32 * 4 + 1, 16 * 4 + 2, 32 * 4 + 2};
-    if (A.elem_bytes == 8) candidates.push_back(64 * 4 + 1);  // pair boxes: ZU = 64 too
+    if (A.elem_bytes == 8) {  // pair boxes: ZU = 64 too
+        candidates.push_back(64 * 4 + 1);
+        candidates.push_back(64 * 4 + 2);
+    }
     if (!tune) best = 16 * 4 + 1;
     if (!best) {
         float best_ms = 1e30f;
