@@ -208,7 +208,13 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
         candidates.push_back(64 * 4 + 1);
         candidates.push_back(64 * 4 + 2);
     }
-    if (!tune) best = 16 * 4 + 1;
+    if (!tune) {  // batched scans: ZU = 32 where its box ring still lets two CTAs share an SM, else 16
+        FdkTmaArgs T = A;
+        T.zu = 32;
+        T.passes = 1;
+        SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
+        best = (fdk_tma_choose(T) && fdk_tma_fits_two_ctas(T)) ? 32 * 4 + 1 : 16 * 4 + 1;
+    }
     if (!best) {
         float best_ms = 1e30f;
         cudaEvent_t e0, e1;
@@ -989,11 +995,12 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::vector<size_t> class_begin;
     for (int ecls : {8, 4, 2}) {  // element size: FP32 pairs, FP32, BF16
-        for (int W : {32, 64, 128}) {
+        for (int cls = 0; cls < 6; cls++) {  // box width 32/64/128 x voxels per thread along z 16/32
+            const int W = 32 << (cls % 3), zu = 16 << (cls / 3);
             std::vector<int> order;
             int box_bytes = 0;
             for (int i = 0; i < n; i++)
-                if (scans[i].W == W && scans[i].elem_bytes == ecls) {
+                if (scans[i].W == W && scans[i].elem_bytes == ecls && scans[i].zu == zu) {
                     order.push_back(i);
                     box_bytes = std::max(box_bytes, scans[i].box_bytes);
                 }
@@ -1003,6 +1010,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
             FdkBatchArgs C{};
             C.nscans = n;
             C.W = W;
+            C.zu = zu;
             C.box_bytes = box_bytes;
             C.elem_bytes = elem;
             C.vps = 4;
@@ -1020,7 +1028,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         }
     }
     SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
-    SGB_REQUIRE(B->classes.size() <= 6, "batch_fdk: too many box classes");
+    SGB_REQUIRE(B->classes.size() <= 6, "batch_fdk: more than 6 box classes");
     for (size_t c = 0; c < B->classes.size(); c++) {
         FdkBatchArgs &C = B->classes[c];
         C.scans = B->scans.as<FdkTmaArgs>();

@@ -196,7 +196,7 @@ int launch_batch_t(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, c
 
 template <typename TP, int BW>
 int batch_occupancy(const FdkBatchArgs &B) {
-    auto k = batch_kernel_for<TP, 16, BW>(B.vps);
+    auto k = B.zu == 32 ? batch_kernel_for<TP, 32, BW>(B.vps) : batch_kernel_for<TP, 16, BW>(B.vps);
     const size_t smem = fdk_batch_smem(B);
     int n = 0;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
@@ -222,18 +222,22 @@ int fdk_batch_ctas_per_sm(const FdkBatchArgs &B) {
                      : (B.W == 64 ? batch_occupancy<__nv_bfloat16, 64>(B) : batch_occupancy<__nv_bfloat16, 128>(B));
 }
 
+template <typename TP, int ZU>
+int launch_batch_z(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
+    return B.W == 32 ? launch_batch_t<TP, ZU, 32>(B, maps, nctas, st)
+                     : (B.W == 64 ? launch_batch_t<TP, ZU, 64>(B, maps, nctas, st)
+                                  : launch_batch_t<TP, ZU, 128>(B, maps, nctas, st));
+}
+
+template <typename TP>
+int launch_batch_tp(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
+    return B.zu == 32 ? launch_batch_z<TP, 32>(B, maps, nctas, st) : launch_batch_z<TP, 16>(B, maps, nctas, st);
+}
+
 int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
-    if (B.elem_bytes == 8)
-        return B.W == 32 ? launch_batch_t<float2, 16, 32>(B, maps, nctas, st)
-                         : (B.W == 64 ? launch_batch_t<float2, 16, 64>(B, maps, nctas, st)
-                                      : launch_batch_t<float2, 16, 128>(B, maps, nctas, st));
-    if (B.elem_bytes == 4)
-        return B.W == 32 ? launch_batch_t<float, 16, 32>(B, maps, nctas, st)
-                         : (B.W == 64 ? launch_batch_t<float, 16, 64>(B, maps, nctas, st)
-                                      : launch_batch_t<float, 16, 128>(B, maps, nctas, st));
-    return B.W == 32 ? launch_batch_t<__nv_bfloat16, 16, 32>(B, maps, nctas, st)
-                     : (B.W == 64 ? launch_batch_t<__nv_bfloat16, 16, 64>(B, maps, nctas, st)
-                                  : launch_batch_t<__nv_bfloat16, 16, 128>(B, maps, nctas, st));
+    if (B.elem_bytes == 8) return launch_batch_tp<float2>(B, maps, nctas, st);
+    if (B.elem_bytes == 4) return launch_batch_tp<float>(B, maps, nctas, st);
+    return launch_batch_tp<__nv_bfloat16>(B, maps, nctas, st);
 }
 
 }  // namespace sgb

@@ -41,7 +41,8 @@ struct FdkBatchArgs {
     int W;                    // common compile-time box width (32 or 64)
     int box_bytes;            // largest box of the batch
     int elem_bytes;
-    int vps;                  // views per pipeline stage (4 or 2)
+    int vps;                  // views per pipeline stage (4, 2 or 1)
+    int zu;                   // voxels per thread along z of every scan in the launch (16 or 32)
 };
 size_t fdk_batch_smem(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B);
@@ -51,6 +52,8 @@ int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas,
 int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st);
 // Picks views-per-stage for the staged box; false when no ring fits shared memory.
 bool fdk_tma_choose(FdkTmaArgs &A);
+// The chosen ring leaves room for two CTAs per SM.
+bool fdk_tma_fits_two_ctas(const FdkTmaArgs &A);
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage);
 // 3D tensor map over the filtered projections (pitch, nt, na).
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map);
