@@ -47,6 +47,13 @@ struct FdkBatchArgs {
 size_t fdk_batch_smem(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B);
 int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+// one storage form each (sgb_fdk_batch_<form>.cu)
+int launch_fdk_batch_pair(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+int launch_fdk_batch_f32(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+int launch_fdk_batch_bf16(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+int fdk_batch_ctas_per_sm_pair(const FdkBatchArgs &B);
+int fdk_batch_ctas_per_sm_f32(const FdkBatchArgs &B);
+int fdk_batch_ctas_per_sm_bf16(const FdkBatchArgs &B);
 
 // Sizes the detector box over every (tile, view) of the geometry (device pre-pass).
 int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st);
