@@ -248,8 +248,12 @@ SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
 /* Execution layout of a plan (no counterpart in the reference): info[0] = 1 when FDK
  * back-projection uses the TMA-staged kernel, info[1..2] = staged box (samples),
  * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z,
- * info[5] (when n >= 6) = launches the views are split over. */
+ * info[5] (when n >= 6) = launches the views are split over, info[6] (when n >= 7) = bytes per
+ * stored filtered sample (8: FP32 pairs (y, y[next] - y), 4: FP32, 2: BF16). */
 SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
+/* Overrides the autotuner's choice of how many launches an FDK plan splits its views over (the
+ * later launches add to the volume); 1 <= passes <= min(8, na).  Results agree to rounding. */
+SGB_API int sgb_plan_set_view_passes(sgb_plan *plan, int passes);
 
 /* ------------------------------------------------------- learned filter */
 /* No counterpart in the reference.  A per-row 1D CNN (5 conv layers, kernel 9, 32

@@ -483,6 +483,14 @@ int sgb_plan_sync(sgb_plan *P, void *stream) {
     return filter_status(f[3]);
 }
 
+int sgb_plan_set_view_passes(sgb_plan *P, int passes) {
+    SGB_REQUIRE(P && P->ct, "plan_set_view_passes: needs an FDK plan");
+    SGB_REQUIRE(passes >= 1 && passes <= 8, "plan_set_view_passes: passes must be in [1, 8], got %d", passes);
+    SGB_REQUIRE(passes <= P->cg.na, "plan_set_view_passes: more passes than views");
+    P->targs.passes = passes;
+    return SGB_OK;
+}
+
 int sgb_plan_info(const sgb_plan *P, int *info, int n) {
     SGB_REQUIRE(P && info && n >= 5, "plan_info: bad argument");
     info[0] = P->tma ? 1 : 0;
@@ -491,6 +499,7 @@ int sgb_plan_info(const sgb_plan *P, int *info, int n) {
     info[3] = P->pitch;
     info[4] = P->targs.zu;
     if (n >= 6) info[5] = P->targs.passes;
+    if (n >= 7) info[6] = P->ct ? P->targs.elem_bytes : 4;
     return SGB_OK;
 }
 

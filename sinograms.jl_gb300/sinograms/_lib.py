@@ -92,6 +92,7 @@ _SIGS = {
     "sgb_plan_last_timing": (c_int, [P, P, c_int]),
     "sgb_plan_info": (c_int, [P, P, c_int]),
     "sgb_plan_sync": (c_int, [P, P]),
+    "sgb_plan_set_view_passes": (c_int, [P, c_int]),
     "sgb_lf_create": (c_int, [c_float, P, ctypes.c_ulonglong, P]),
     "sgb_lf_num_params": (c_int, [P]),
     "sgb_lf_get_params": (c_int, [P, P, P]),

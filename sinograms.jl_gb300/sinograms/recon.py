@@ -73,9 +73,14 @@ class _Plan:
 
     def info(self) -> dict:
         """Execution layout: TMA-staged FDK kernel in use, staged box, row pitch, z-unroll."""
-        a = np.zeros(6, dtype=np.int32)
-        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 6), "plan_info")
-        return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]), view_passes=int(a[5]))
+        a = np.zeros(7, dtype=np.int32)
+        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 7), "plan_info")
+        return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]), view_passes=int(a[5]),
+                    sample_bytes=int(a[6]))
+
+    def set_view_passes(self, passes: int):
+        """FDK plans: split the views over `passes` launches (overrides the autotuner's choice)."""
+        _status(_lib.lib().sgb_plan_set_view_passes(self._h, int(passes)), "plan_set_view_passes")
 
     def sync(self):
         """Wait for torch's current stream and raise the device errors of asynchronous calls."""

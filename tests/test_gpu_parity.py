@@ -351,3 +351,32 @@ def test_async_host_plan_calls_match_blocking(cuda):
         S.fbp(plan2, hs.numpy(), out=out2.numpy(), sync=False)
         plan2.sync()
     assert np.array_equal(out2.numpy(), ref2)
+
+
+@pytest.mark.parametrize("passes", [2, 3])
+def test_fdk_view_passes_agree(cuda, passes):
+    """Views split over several launches (the later ones add to the volume) give the one-launch
+    result to rounding and the oracle's."""
+    f, c = fix("fdk_flat"), C.FDK_FLAT
+    plan = S.plan_fbp(C.to_geom(c["rg"]), C.to_image(c["ig"]), window=S.Window(c["window"]))
+    assert plan.info()["tma"], plan.info()
+    plan.set_view_passes(1)
+    one = S.fdk(plan, f["proj"])
+    plan.set_view_passes(passes)
+    assert plan.info()["view_passes"] == passes
+    split = S.fdk(plan, f["proj"])
+    assert O.rel_rmse(split, one) < 1e-6
+    close(split, f["ref"])
+
+
+def test_fdk_pair_boxes_too_large_fall_back_to_fp32_boxes(cuda):
+    """A 16 x 16 x 16 voxel tile of 2 mm voxels at magnification up to ~1.9 needs a box of 128 x ~66
+    samples: four pair (8-byte) stages exceed shared memory, four FP32 stages fit."""
+    rg = C.ct("flat", ns=256, nt=128, ds=1.0, dt=1.0, na=48, dsd=300.0, dod=100.0)
+    ig = dict(dims=(32, 32, 16), deltas=(2.0, 2.0, 2.0))
+    proj = O.ellipsoid_proj(rg, C.ELL3).astype(np.float32)
+    ref = O.fdk(rg, ig, proj)
+    plan = S.plan_fbp(C.to_geom(rg), C.to_image(ig))
+    info = plan.info()
+    assert info["tma"] and info["sample_bytes"] == 4 and info["box"][0] == 128, info
+    close(S.fdk(plan, proj), ref)
