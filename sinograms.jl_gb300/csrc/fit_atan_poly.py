@@ -1,6 +1,7 @@
-"""Coefficients of the arc-detector angle polynomial used by the 2D fan back-projector.
+"""Coefficients of the arc-detector angle polynomials used by the 2D fan back-projector.
 
-atan(q) ~ q * P(q^2) on |q| <= 1, P of degree 8: minimax in absolute error, found by Lawson's
+atan(q) ~ q * P(q^2) on |q| <= 1 (P of degree 8) and on |q| <= 0.6 (degree 5, for detectors within
++-31 deg): minimax in absolute error, found by Lawson's
 iteratively reweighted least squares (C. L. Lawson, 1961) from a least-squares start on a dense
 grid.  Running this prints the coefficients as they appear in `sgb_back.cu` and the float32
 Horner error against numpy's double atan (about 1.1e-7 rad, i.e. 1e-4 detector bins at
@@ -32,8 +33,11 @@ def horner_f32(c: np.ndarray, q: np.ndarray) -> np.ndarray:
 
 
 if __name__ == "__main__":
-    c = fit()
-    for k, v in enumerate(c):
-        print(f"c{k} = {np.float32(v)!r}")
-    q = np.linspace(-1.0, 1.0, 400001)
-    print("max abs error (float32 Horner):", float(np.max(np.abs(horner_f32(c, q) - np.arctan(q)))))
+    # atan_poly (|q| <= 1, 9 terms, 1.1e-7 rad) and atan_poly6 (|q| <= 0.6, 6 terms, 8.0e-8 rad)
+    for qmax, n in ((1.0, 9), (0.6, 6)):
+        c = fit(qmax, n)
+        print(f"|q| <= {qmax}, {n} terms:")
+        for k, v in enumerate(c):
+            print(f"  c{k} = {np.float32(v)!r}")
+        q = np.linspace(-qmax, qmax, 400001)
+        print("  max abs error (float32 Horner):", float(np.max(np.abs(horner_f32(c, q) - np.arctan(q)))))

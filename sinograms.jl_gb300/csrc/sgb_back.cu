@@ -154,7 +154,7 @@ int launch_fdk_z(const FdkArgs &A, cudaStream_t st) {
 // operations per tap.  Small images split the views over a cluster of G CTAs (grid z =
 // slice * G + rank); their partial tiles are summed through distributed shared memory in rank
 // order.
-enum { B2_PAR = 0, B2_FLAT = 1, B2_ARC = 2, B2_ARC_EXACT = 3 };
+enum { B2_PAR = 0, B2_FLAT = 1, B2_ARC = 2, B2_ARC_EXACT = 3, B2_ARC_NARROW = 4 };
 enum { V_FAST = 0, V_CHECKED = 1, V_GLOBAL = 2, V_NONE = 3 };
 constexpr int kB2X = 32, kB2Y = 8, kB2P = 4, kB2T = kB2Y * kB2P;  // tile 32 x 32
 constexpr int kB2V = 32;   // views per chunk
@@ -190,6 +190,18 @@ __device__ __forceinline__ float atan_poly(float q) {
     return p * q;
 }
 
+// The same on |q| <= 0.6 with 6 terms (8.0e-8 rad), for detectors within +-31 deg.
+__device__ __forceinline__ float atan_poly6(float q) {
+    const float t = q * q;
+    float p = -3.794763982e-02f;
+    p = fmaf(p, t, 9.173785150e-02f);
+    p = fmaf(p, t, -1.391045451e-01f);
+    p = fmaf(p, t, 1.996324360e-01f);
+    p = fmaf(p, t, -3.333176374e-01f);
+    p = fmaf(p, t, 9.999998212e-01f);
+    return p * q;
+}
+
 // per-(column, view) terms: parallel a = x cos + wb; fan a = dso + x sin, b = x cos - so
 template <int M>
 __device__ __forceinline__ void b2_col(const Back2Args &A, float x, float sb, float cb, float *a, float *b) {
@@ -203,8 +215,9 @@ __device__ __forceinline__ void b2_col(const Back2Args &A, float x, float sb, fl
 }
 
 // detector bin bb and weight w2 of the pixel row y; `front`: d > 0 (fan); `inside`: false
-// only for the arc polynomial when d <= 0 or |r/d| > 1, where the true tap is off the
-// detector (the launcher uses the polynomial only for detectors narrower than +-45 deg)
+// only for the arc polynomials when d <= 0 or |r/d| exceeds their range (1, or 0.6 for the
+// narrow one), where the true tap is off the detector: the launcher uses them only for
+// detectors narrower than +-45 deg (+-31 deg), with a 4-bin margin
 template <int M>
 __device__ __forceinline__ float b2_pix(const Back2Args &A, float a, float b, float y, float sb, float cb,
                                         float *w2, bool *front, bool *inside) {
@@ -228,6 +241,10 @@ __device__ __forceinline__ float b2_pix(const Back2Args &A, float a, float b, fl
     float rd = rcp_approx(d);
     rd = fmaf(rd, fmaf(-d, rd, 1.f), rd);
     const float q = r * rd;
+    if (M == B2_ARC_NARROW) {
+        *inside = *front && fabsf(q) <= 0.6f;
+        return fmaf(A.dsd_ds, atan_poly6(q), A.wb);
+    }
     *inside = *front && fabsf(q) <= 1.f;
     return fmaf(A.dsd_ds, atan_poly(q), A.wb);
 }
@@ -486,9 +503,10 @@ int launch_back2(const Back2Args &A, cudaStream_t st) {
     switch (A.mode) {
     case SGB_PAR: return launch_back2_mode<B2_PAR>(A, st);
     case SGB_ARC: {
-        // the angle polynomial covers |r/d| <= 1: detectors whose taps stay inside +-45 deg
-        // (with a 4-bin margin) use it, wider ones atan2f
+        // the angle polynomials cover |r/d| <= 0.6 (6 terms) and <= 1 (9 terms): detectors whose
+        // taps stay inside +-atan(0.6) or +-45 deg (with a 4-bin margin) use them, wider ones atan2f
         const double half = (std::max(std::fabs(1.0 - A.wb), std::fabs((double)A.nb - A.wb)) + 4.0) / A.dsd_ds;
+        if (half < 0.5404195002705842) return launch_back2_mode<B2_ARC_NARROW>(A, st);
         return half < 0.7853981633974483 ? launch_back2_mode<B2_ARC>(A, st) : launch_back2_mode<B2_ARC_EXACT>(A, st);
     }
     default: return launch_back2_mode<B2_FLAT>(A, st);
