@@ -93,6 +93,29 @@ def _issue_roofline(updates, back_ms, clocks):
             "frac": achieved / peak, "source": "profiles/fdk_tma_kernel_bench_issue.md (ncu smsp__inst_executed)"}
 
 
+def _bp_roofline(updates, back_ms):
+    """The back-projection bound of the task's scope table: R_bp = min(P_fp32 / F_upd,
+    BW_smem / B_upd), with F_upd = 15 FP32 flops and B_upd = 4 taps x 4 B from shared memory per
+    update, and P_fp32, BW_smem measured on this GPU by the library's microbenchmarks.  The
+    FP32 form stores (y, y[next] - y) pairs, so it actually loads one or two 8-byte pairs per
+    update (one in the streaming form), not four 4-byte taps."""
+    import sinograms as S
+    try:
+        pk = S.measure_peaks()
+    except Exception as e:  # the headline line must still print
+        return {"error": f"{type(e).__name__}: {e}"}
+    b_upd = 16.0
+    r_fp32 = pk["fp32_flops_per_s"] / F_UPD
+    r_smem = pk["smem_load_bytes_per_s"] / b_upd
+    achieved = updates / (back_ms / 1e3)
+    return {"unit": UNIT, "flops_per_update": F_UPD, "measured_fp32_tflops": pk["fp32_flops_per_s"] / 1e12,
+            "fp32_bound": r_fp32, "smem_bytes_per_update": b_upd,
+            "measured_smem_load_tbs": pk["smem_load_bytes_per_s"] / 1e12, "smem_bound": r_smem,
+            "smem_bytes_per_update_as_loaded": "8 (streaming form, one (y, dy) pair) to 16 (four-tap form, two pairs)",
+            "r_bp": min(r_fp32, r_smem), "achieved": achieved, "frac": achieved / min(r_fp32, r_smem),
+            "source": "sgb_measure_peaks (conflict-free 16-byte shared loads; 8 independent FMA chains)"}
+
+
 def _filter_roofline(form, peaks):
     """Tensor-core work of the ramp filter (split-BF16 GEMM on first differences): 2 x rows x
     K x N x products, K = ns rounded up to 32, N = the output columns the MMAs compute
@@ -292,6 +315,7 @@ def run_ours(args):
                                     "achieved_tflops": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12,
                                     "peak_tflops_nominal": NOMINAL_FP32_TFLOPS,
                                     "frac": F_UPD * upd / (f["back_ms"] / 1e3) / 1e12 / NOMINAL_FP32_TFLOPS}},
+        "bp_roofline": _bp_roofline(upd, f["back_ms"]),
         "filter_roofline": _filter_roofline(forms[head], peaks),
         "plan": forms[head]["plan"].info(),
         "gpu_launches": f["gpu_launches"],
@@ -423,8 +447,24 @@ def measure_2d(args):
             plan, lf.apply(LF.fbp_filter_rows(plan, s, sync=False), sync=False), sync=False), reps)
         z = LF.fbp_filter_rows(plan, s)
         ms_net = _per_call_ms(lambda: lf.apply(z, sync=False), reps)
+        # forward FLOPs: 2 per multiply-add over the 5 layers (1->32, 3 x 32->32, 32->1, kernel 9)
+        net_flops = 2.0 * z.numel() * 9 * (32 + 3 * 32 * 32 + 32)
+        # distance-driven projection of a 512^2 image over the scan's 90 views; FLOPs per the fixed
+        # count na * nPix * (2 nPix + 7 (nDet + 1))
+        img0 = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000))
+        ms_dd = _per_call_ms(lambda: LF.dd_project(img0, geo), reps)
+        dd_flops = float(len(geo.angle) * geo.nPix * (2 * geo.nPix + 7 * (geo.nDet + 1)))
+        try:
+            fp32_peak = S.measure_peaks()["fp32_flops_per_s"]
+        except Exception:
+            fp32_peak = None
         out["learned_filter_flat_888x90"] = {
             "ms_plain_fbp": ms_plain, "ms_learned_fbp": ms_learned, "ms_network": ms_net,
+            "network_tflops": net_flops / (ms_net / 1e3) / 1e12,
+            "network_frac_of_bf16_peak": net_flops / (ms_net / 1e3) / (_peaks().get("bf16_tflops", 1941.6) * 1e12),
+            "dd_project_ms": ms_dd, "dd_project_call": "blocking (includes one stream synchronisation)",
+            "dd_project_tflops": dd_flops / (ms_dd / 1e3) / 1e12,
+            "dd_project_frac_of_fp32": (dd_flops / (ms_dd / 1e3) / fp32_peak) if fp32_peak else None,
             "rmse_vs_phantom_plain": float(np.mean(rp)), "rmse_vs_phantom_learned": float(np.mean(rl)),
             "judge_kept_learned": f"{kept}/8", "weights": os.path.basename(LF.default_weights_path())}
     except Exception as e:  # the headline line must still print

@@ -254,6 +254,10 @@ SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
 /* Overrides the autotuner's choice of how many launches an FDK plan splits its views over (the
  * later launches add to the volume); 1 <= passes <= min(8, na).  Results agree to rounding. */
 SGB_API int sgb_plan_set_view_passes(sgb_plan *plan, int passes);
+/* On-chip peaks the back-projectors' roofline is stated against (no reference counterpart),
+ * measured on `stream` with CUDA events: peaks[0] = shared-memory load bandwidth (bytes/s,
+ * conflict-free 16-byte loads), peaks[1] = FP32 FMA throughput (flop/s, an FMA counting 2). */
+SGB_API int sgb_measure_peaks(double *peaks, int n, void *stream);
 
 /* ------------------------------------------------------- learned filter */
 /* No counterpart in the reference.  A per-row 1D CNN (5 conv layers, kernel 9, 32

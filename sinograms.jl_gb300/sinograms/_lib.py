@@ -93,6 +93,7 @@ _SIGS = {
     "sgb_plan_info": (c_int, [P, P, c_int]),
     "sgb_plan_sync": (c_int, [P, P]),
     "sgb_plan_set_view_passes": (c_int, [P, c_int]),
+    "sgb_measure_peaks": (c_int, [P, c_int, P]),
     "sgb_lf_create": (c_int, [c_float, P, ctypes.c_ulonglong, P]),
     "sgb_lf_num_params": (c_int, [P]),
     "sgb_lf_get_params": (c_int, [P, P, P]),
@@ -149,6 +150,14 @@ def check(status: int, what: str = "") -> None:
 
 def launch_count() -> int:
     return int(lib().sgb_launch_count())
+
+
+def measure_peaks(stream=None) -> dict:
+    """On-chip peaks measured on the GPU: shared-memory load bandwidth (bytes/s) and FP32 FMA
+    throughput (flop/s)."""
+    out = (ctypes.c_double * 2)()
+    check(lib().sgb_measure_peaks(out, 2, stream), "measure_peaks")
+    return {"smem_load_bytes_per_s": float(out[0]), "fp32_flops_per_s": float(out[1])}
 
 
 def exported_symbols() -> list[str]:
