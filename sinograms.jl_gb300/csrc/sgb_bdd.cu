@@ -96,36 +96,48 @@ __device__ __forceinline__ void row_affine(const ViewInfo &vi, int r, int nPix, 
 // forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info, ascending knots K
 // (nDet+1), per-bin integrals B (nDet, ascending order: sino * L * |ddetm|, signed as the
 // reference's prefix, :196) and 1/(K[j+1]-K[j]) (reversed when detm descends, :198-202).
-__global__ void bdd_setup_kernel(BddArgs G, ViewInfo *info, float *detm, float *L, const float *sino, float *kn,
-                                 float *kb, float *kinv) {
+// One CTA per (view, chunk of kSetupChunk bins): the view's constants once, each FP64 boundary
+// once into shared memory, then the chunk's outputs from those values (the same FP64 calls).
+constexpr int kSetupChunk = kThreads;
+__global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo *info, float *detm, float *L,
+                                                             const float *sino, float *kn, float *kb, float *kinv) {
+    __shared__ ViewInfo vis;
+    __shared__ int desc_s;
+    __shared__ double bnd[kSetupChunk + 1];
     const int p = blockIdx.x, nDet = G.nDet;
+    const int n0 = blockIdx.y * kSetupChunk, n1 = min(nDet, n0 + kSetupChunk), cnt = n1 - n0;
     const double beta = G.angle[p];
-    const ViewInfo vi = view_info(beta, G.DS0);
-    if (threadIdx.x == 0) info[p] = vi;
+    if (threadIdx.x == 0) {
+        vis = view_info(beta, G.DS0);
+        if (blockIdx.y == 0) info[p] = vis;
+        desc_s = sino ? det_boundary(vis, beta, 0, nDet, G.DSD, G.DS0, G.dSize) >
+                            det_boundary(vis, beta, 1, nDet, G.DSD, G.DS0, G.dSize)
+                      : 0;
+    }
+    __syncthreads();
+    const ViewInfo vi = vis;
+    const bool desc = desc_s != 0;
+    // boundaries b0 .. b0 + cnt: those of bins n0 .. n1-1 (reversed for a descending back-projection)
+    const int b0 = desc ? nDet - n1 : n0;
+    for (int i = threadIdx.x; i <= cnt; i += blockDim.x)
+        bnd[i] = det_boundary(vi, beta, b0 + i, nDet, G.DSD, G.DS0, G.dSize);
+    __syncthreads();
     if (!sino) {
         float *dm = detm + (size_t)p * (nDet + 1);
-        for (int k = threadIdx.x; k <= nDet; k += blockDim.x)
-            dm[k] = (float)det_boundary(vi, beta, k, nDet, G.DSD, G.DS0, G.dSize);
-        for (int n = threadIdx.x; n < nDet; n += blockDim.x) {
-            const double d0 = det_boundary(vi, beta, n, nDet, G.DSD, G.DS0, G.dSize);
-            const double d1 = det_boundary(vi, beta, n + 1, nDet, G.DSD, G.DS0, G.dSize);
-            L[(size_t)p * nDet + n] = (float)det_scale(vi, d0, d1, G.pSize);
-        }
+        for (int k = n0 + threadIdx.x; k <= n1; k += blockDim.x) dm[k] = (float)bnd[k - n0];
+        for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x)
+            L[(size_t)p * nDet + n] = (float)det_scale(vi, bnd[n - n0], bnd[n + 1 - n0], G.pSize);
         return;
     }
-    const double d_first = det_boundary(vi, beta, 0, nDet, G.DSD, G.DS0, G.dSize);
-    const double d_second = det_boundary(vi, beta, 1, nDet, G.DSD, G.DS0, G.dSize);
-    const bool desc = d_first > d_second;
     float *K = kn + (size_t)p * (nDet + 1), *B = kb + (size_t)p * nDet, *KI = kinv + (size_t)p * nDet;
-    for (int k = threadIdx.x; k <= nDet; k += blockDim.x) {
+    for (int k = n0 + threadIdx.x; k <= n1; k += blockDim.x) {
         const int src = desc ? nDet - k : k;
-        K[k] = (float)det_boundary(vi, beta, src, nDet, G.DSD, G.DS0, G.dSize);
+        K[k] = (float)bnd[src - b0];
     }
-    for (int j = threadIdx.x; j < nDet; j += blockDim.x) {
+    for (int j = n0 + threadIdx.x; j < n1; j += blockDim.x) {
         // ascending bin j covers reference bin n = desc ? nDet-1-j : j
         const int n = desc ? nDet - 1 - j : j;
-        const double d0 = det_boundary(vi, beta, n, nDet, G.DSD, G.DS0, G.dSize);
-        const double d1 = det_boundary(vi, beta, n + 1, nDet, G.DSD, G.DS0, G.dSize);
+        const double d0 = bnd[n - b0], d1 = bnd[n + 1 - b0];
         const double w = ((double)sino[p + (size_t)G.na * n] * det_scale(vi, d0, d1, G.pSize)) * (d1 - d0);
         B[j] = (float)(desc ? -w : w);  // integral over the bin in the ascending direction
         KI[j] = (float)(1.0 / std::fabs(d1 - d0));
@@ -300,9 +312,12 @@ int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void
     float *detm = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
     float *L = detm + (size_t)G.na * (G.nDet + 1);
     SGB_CUDA(cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)G.na * G.nDet, st));
-    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, detm, L, nullptr, nullptr, nullptr, nullptr);
+    bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L, nullptr,
+                                                                                             nullptr, nullptr, nullptr);
     SGB_TRY(after_launch("bdd_setup_kernel"));
-    int rsplit = std::max(1, std::min((G.nPix + kWarps - 1) / kWarps, (2 * 152 + G.na - 1) / G.na));
+    // rows split over CTAs so that each SM holds ~8 of them (views x row blocks)
+    const int target = 8 * std::max(1, num_sms());
+    int rsplit = std::max(1, std::min((G.nPix + kWarps - 1) / kWarps, (target + G.na - 1) / G.na));
     int rows = (G.nPix + rsplit - 1) / rsplit;
     rows = (rows + kWarps - 1) / kWarps * kWarps;
     rsplit = (G.nPix + rows - 1) / rows;
@@ -322,10 +337,13 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
     float *kb = kn + (size_t)G.na * (G.nDet + 1);
     float *kinv = kb + (size_t)G.na * G.nDet;
     SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
-    bdd_setup_kernel<<<G.na, kThreads, 0, st>>>(G, info, nullptr, nullptr, sino, kn, kb, kinv);
+    bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, nullptr, nullptr,
+                                                                                             sino, kn, kb, kinv);
     SGB_TRY(after_launch("bdd_setup_kernel"));
     int gx = (G.nPix + kWarps - 1) / kWarps;
-    int vsplit = std::max(1, std::min(G.na, (2 * 152 + gx - 1) / gx));
+    // views split over CTAs so that each SM holds ~8 of them (row blocks x view groups)
+    const int target = 8 * std::max(1, num_sms());
+    int vsplit = std::max(1, std::min(G.na, (target + gx - 1) / gx));
     int vpc = (G.na + vsplit - 1) / vsplit;
     vsplit = (G.na + vpc - 1) / vpc;
     SGB_CUDA(cudaFuncSetAttribute(bdd_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
