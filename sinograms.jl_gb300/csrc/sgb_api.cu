@@ -208,12 +208,20 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
         candidates.push_back(64 * 4 + 1);
         candidates.push_back(64 * 4 + 2);
     }
-    if (!tune) {  // batched scans: ZU = 32 where its box ring still lets two CTAs share an SM, else 16
-        FdkTmaArgs T = A;
-        T.zu = 32;
-        T.passes = 1;
-        SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
-        best = (fdk_tma_choose(T) && fdk_tma_fits_two_ctas(T)) ? 32 * 4 + 1 : 16 * 4 + 1;
+    if (!tune) {  // batched scans: the largest ZU (64 for pair boxes, 32) whose box ring still lets two
+                  // CTAs share an SM, else 16
+        best = 16 * 4 + 1;
+        for (int zu : {64, 32}) {
+            if (zu == 64 && A.elem_bytes != 8) continue;
+            FdkTmaArgs T = A;
+            T.zu = zu;
+            T.passes = 1;
+            SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
+            if (fdk_tma_choose(T) && fdk_tma_fits_two_ctas(T)) {
+                best = zu * 4 + 1;
+                break;
+            }
+        }
     }
     if (!best) {
         float best_ms = 1e30f;
@@ -939,7 +947,7 @@ struct sgb_batch {
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t ev[8] = {};  // graph event nodes: start, filters done, each class done
+    cudaEvent_t ev[12] = {};  // graph event nodes: start, filters done, each class done
     ~sgb_batch() {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
@@ -1004,7 +1012,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::vector<size_t> class_begin;
     for (int ecls : {8, 4, 2}) {  // element size: FP32 pairs, FP32, BF16
-        for (int cls = 0; cls < 6; cls++) {  // box width 32/64/128 x voxels per thread along z 16/32
+        for (int cls = 0; cls < 9; cls++) {  // box width 32/64/128 x voxels per thread along z 16/32/64
             const int W = 32 << (cls % 3), zu = 16 << (cls / 3);
             std::vector<int> order;
             int box_bytes = 0;
@@ -1037,7 +1045,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         }
     }
     SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
-    SGB_REQUIRE(B->classes.size() <= 6, "batch_fdk: more than 6 box classes");
+    SGB_REQUIRE(B->classes.size() <= 10, "batch_fdk: more than 10 box classes");
     for (size_t c = 0; c < B->classes.size(); c++) {
         FdkBatchArgs &C = B->classes[c];
         C.scans = B->scans.as<FdkTmaArgs>();

@@ -197,6 +197,8 @@ int launch_batch_t(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, c
 template <typename TP, int BW>
 int batch_occupancy_w(const FdkBatchArgs &B) {
     auto k = B.zu == 32 ? batch_kernel_for<TP, 32, BW>(B.vps) : batch_kernel_for<TP, 16, BW>(B.vps);
+    if constexpr (sizeof(TP) == 8)
+        if (B.zu == 64) k = batch_kernel_for<TP, 64, BW>(B.vps);
     const size_t smem = fdk_batch_smem(B);
     int n = 0;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;
@@ -214,6 +216,8 @@ int launch_batch_z(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, c
 
 template <typename TP>
 int launch_batch_tp(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
+    if constexpr (sizeof(TP) == 8)  // ZU = 64 only for pair boxes
+        if (B.zu == 64) return launch_batch_z<TP, 64>(B, maps, nctas, st);
     return B.zu == 32 ? launch_batch_z<TP, 32>(B, maps, nctas, st) : launch_batch_z<TP, 16>(B, maps, nctas, st);
 }
 

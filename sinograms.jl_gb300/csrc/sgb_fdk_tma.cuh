@@ -42,7 +42,7 @@ struct FdkBatchArgs {
     int box_bytes;            // largest box of the batch
     int elem_bytes;
     int vps;                  // views per pipeline stage (4, 2 or 1)
-    int zu;                   // voxels per thread along z of every scan in the launch (16 or 32)
+    int zu;                   // voxels per thread along z of every scan in the launch (16, 32, 64)
 };
 size_t fdk_batch_smem(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B);
