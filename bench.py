@@ -392,8 +392,9 @@ def measure_2d(args):
     """The 2D workloads beside the headline, device-resident, on seeded synthetic inputs:
     SinoPar 256 x 180 -> 256^2 with a Hann window; SinoFanArc 888 x 512 views over a short scan ->
     512^2 (Parker weights, 0.5% noise); and the learned row filter's sparse-view scan (888 x 90
-    views over 360 deg -> 512^2, flat detector): plain against learned FBP time, and image RMSE
-    against the phantom on 8 held-out scans."""
+    views over 360 deg -> 512^2, flat detector): plain FBP against FBP with the CNN row filter and
+    with the learned linear (ramp) filter, time and image RMSE against the phantom on 8 held-out
+    scans."""
     import torch
 
     import sinograms as S
@@ -431,18 +432,23 @@ def measure_2d(args):
         geo = S.BddGeo.from_geoms(rg, ig)
         mask = torch.as_tensor(ig.mask, device="cuda")
         gen = torch.Generator(device="cuda").manual_seed(900000)
-        rp, rl, kept = [], [], 0
+        ramp = LF.LearnedRamp.load(LF.default_ramp_path())
+        plan_ramp = ramp.plan(rg, ig)
+        rp, rl, rr, kept, kept_r = [], [], [], 0, 0
         for i in range(8):
             img = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000 + i))
             s = LF.dd_project(img, geo)
             s = s + 0.005 * s.abs().max() * torch.randn(s.shape, device="cuda", generator=gen)
             rp.append(float((S.fbp(plan, s) - img)[mask].pow(2).mean().sqrt()))
+            rr.append(float((S.fbp(plan_ramp, s) - img)[mask].pow(2).mean().sqrt()))
+            kept_r += int(LF.fbp_learned_ramp(plan_ramp, plan, s)[1]["used"] == "learned")
             im_l, info = LF.fbp_learned(plan, lf, s, judge=True)
             rl.append(float((LF.fbp_backproject(plan, lf.apply(LF.fbp_filter_rows(plan, s))) - img)[mask]
                             .pow(2).mean().sqrt()))
             kept += int(info["used"] == "learned")
         s = s.contiguous()
         ms_plain = _per_call_ms(lambda: S.fbp(plan, s, sync=False), reps)
+        ms_ramp = _per_call_ms(lambda: S.fbp(plan_ramp, s, sync=False), reps)
         ms_learned = _per_call_ms(lambda: LF.fbp_backproject(
             plan, lf.apply(LF.fbp_filter_rows(plan, s, sync=False), sync=False), sync=False), reps)
         z = LF.fbp_filter_rows(plan, s)
@@ -466,7 +472,9 @@ def measure_2d(args):
             "dd_project_tflops": dd_flops / (ms_dd / 1e3) / 1e12,
             "dd_project_frac_of_fp32": (dd_flops / (ms_dd / 1e3) / fp32_peak) if fp32_peak else None,
             "rmse_vs_phantom_plain": float(np.mean(rp)), "rmse_vs_phantom_learned": float(np.mean(rl)),
-            "judge_kept_learned": f"{kept}/8", "weights": os.path.basename(LF.default_weights_path())}
+            "judge_kept_learned": f"{kept}/8", "weights": os.path.basename(LF.default_weights_path()),
+            "ms_learned_ramp_fbp": ms_ramp, "rmse_vs_phantom_learned_ramp": float(np.mean(rr)),
+            "judge_kept_learned_ramp": f"{kept_r}/8", "ramp_gain": os.path.basename(LF.default_ramp_path())}
     except Exception as e:  # the headline line must still print
         out["error"] = f"{type(e).__name__}: {e}"
     return out

@@ -32,7 +32,7 @@ from .bdd import BddGeo
 from .filters import SinogramsArgumentError
 from .geom import ImageGeom, SinoFanFlat, _rfov
 from .phantoms import random_ellipses
-from .recon import FBPNormalPlan, _status, plan_fbp
+from .recon import FBPNormalPlan, _status, fbp, plan_fbp
 
 try:
     import torch
@@ -252,6 +252,99 @@ def fbp_learned(plan: FBPNormalPlan, lf: LearnedFilter, sino, judge: bool = True
     rp = reprojection_residual(img_p, sino, geo)
     used = "learned" if rl <= (1 + tol) * rp else "plain"
     return (img_l if used == "learned" else img_p), {"used": used, "residual_learned": rl, "residual_plain": rp}
+
+
+# ------------------------------------------------------ learned linear (ramp) filter
+
+class LearnedRamp:
+    """Learned linear row filter: the plan's ramp response Hk times a per-frequency gain G(k)
+    fitted on the same self-generated data as the CNN.  G is the least-squares optimum over all
+    real, even, shift-invariant row filters for the CNN's loss (filtered noisy rows against the
+    filtered noise-free rows, evaluated over the full padded row):
+
+        G(k) = sum Re(conj(Wn(k)) Wc(k)) / sum |Wn(k)|^2,
+
+    with Wn, Wc the length-npad FFTs of the zero-padded weighted noisy and noise-free rows (the
+    ramp factor cancels).  Because G only changes the plan's Hk (the `filter` option of plan_fbp,
+    plan2.jl:106-138), FBP with it runs exactly the plain FBP kernels: same launches, same
+    latency."""
+
+    def __init__(self, gain, npad: int, meta: dict | None = None):
+        self.gain = np.asarray(gain, dtype=np.float64)
+        if self.gain.shape != (npad,):
+            raise SinogramsArgumentError(f"gain has shape {self.gain.shape}, expected ({npad},)")
+        self.npad = int(npad)
+        self.meta = dict(meta or {})
+
+    def plan(self, rg, ig, window=None):
+        """plan_fbp(rg, ig; filter = Hk .* G) with Hk the plan's own ramp response."""
+        base = plan_fbp(rg, ig, npad=self.npad) if window is None else plan_fbp(rg, ig, window=window,
+                                                                                npad=self.npad)
+        return plan_fbp(rg, ig, filter=base.filter * self.gain)
+
+    def save(self, path: str):
+        np.savez(path, gain=self.gain, npad=np.int64(self.npad),
+                 **{k: np.asarray(v) for k, v in self.meta.items()})
+
+    @classmethod
+    def load(cls, path: str):
+        d = np.load(path)
+        meta = {k: d[k].item() for k in d.files if k not in ("gain", "npad")}
+        return cls(d["gain"], int(d["npad"]), meta)
+
+
+def fit_learned_ramp(n_phantoms: int, seed: int, rg=None, ig=None, noise: float = 0.005,
+                     chunk: int = 64) -> LearnedRamp:
+    """Fit G(k) on n_phantoms seeded random-ellipse scans (the CNN's data: DD projections
+    plus Gaussian noise of sigma = noise * max(sinogram)).  The weighted rows come from an
+    all-pass plan (Hk = 1), whose filtered rows are the weighted sinogram itself; the spectra
+    are accumulated in float64 on the host."""
+    if rg is None:
+        rg, ig = sparse_fan_geometry()
+    base = plan_fbp(rg, ig)
+    npad = len(base.filter)
+    allpass = plan_fbp(rg, ig, filter=np.ones(npad))
+    geo = BddGeo.from_geoms(rg, ig)
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    ig0 = ig.with_mask(None)
+    cross = np.zeros(npad // 2 + 1)
+    power = np.zeros(npad // 2 + 1)
+    for p0 in range(0, n_phantoms, chunk):
+        p1 = min(n_phantoms, p0 + chunk)
+        s = torch.empty((p1 - p0, rg.na, rg.nb), device="cuda")
+        for i in range(p0, p1):
+            s[i - p0] = dd_project(ellipse_image(ig0, phantom_ellipses(seed * 100003 + i)), geo)
+        peak = s.abs().amax(dim=(1, 2), keepdim=True)
+        sn = s + noise * peak * torch.randn(s.shape, device="cuda", generator=gen)
+        wc = fbp_filter_rows(allpass, s).reshape(-1, rg.nb).cpu().numpy().astype(np.float64)
+        wn = fbp_filter_rows(allpass, sn).reshape(-1, rg.nb).cpu().numpy().astype(np.float64)
+        fc = np.fft.rfft(wc, n=npad, axis=1)
+        fn = np.fft.rfft(wn, n=npad, axis=1)
+        cross += np.sum((fn.conj() * fc).real, axis=0)
+        power += np.sum(np.abs(fn) ** 2, axis=0)
+    half = np.where(power > 0, cross / np.where(power > 0, power, 1.0), 1.0)
+    gain = np.concatenate([half, half[1:npad - npad // 2][::-1]])  # even: G(npad - k) = G(k)
+    return LearnedRamp(gain, npad, {"phantoms": n_phantoms, "seed": seed, "noise": noise})
+
+
+def fbp_learned_ramp(plan_learned: FBPNormalPlan, plan_plain: FBPNormalPlan, sino, judge: bool = True,
+                     tol: float = 0.0):
+    """FBP through the learned-ramp plan, judged as fbp_learned judges the CNN: the learned
+    image is kept only if its DD reprojection residual is at most (1 + tol) times plain ramp
+    FBP's, else plain FBP is returned.  Returns (image, info)."""
+    img_l = fbp(plan_learned, sino)
+    if not judge:
+        return img_l, {"used": "learned"}
+    img_p = fbp(plan_plain, sino)
+    geo = BddGeo.from_geoms(plan_plain.rg, plan_plain.ig)
+    rl = reprojection_residual(img_l, sino, geo)
+    rp = reprojection_residual(img_p, sino, geo)
+    used = "learned" if rl <= (1 + tol) * rp else "plain"
+    return (img_l if used == "learned" else img_p), {"used": used, "residual_learned": rl, "residual_plain": rp}
+
+
+def default_ramp_path() -> str:
+    return os.path.join(WEIGHTS_DIR, "learned_ramp_fanflat888_90v.npz")
 
 
 def default_weights_path() -> str:

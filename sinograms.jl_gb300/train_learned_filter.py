@@ -2,6 +2,10 @@
 kernels) and evaluate it against plain ramp FBP on held-out scans.
 
     python sinograms.jl_gb300/train_learned_filter.py [--phantoms 20000] [--out PATH]
+    python sinograms.jl_gb300/train_learned_filter.py --linear [--phantoms 2000] [--out PATH]
+
+--linear fits the learned linear filter instead (LearnedRamp: the ramp response times the
+least-squares per-frequency gain) and compares it with plain FBP at the same latency.
 
 Data: seeded random-ellipse phantoms (20 ellipses, centres r <= 220 mm, semi-axes
 U[4,120] mm, density U[-0.3,1]) rasterised on the 512^2 grid, projected by the
@@ -72,6 +76,28 @@ def summary(lf, plan, rg, ig, n):
         "latency_ms_plain": lat_plain, "latency_ms_learned": lat_learned}
 
 
+def linear_summary(lr, rg, ig, n, seed=900000):
+    """Held-out image RMSE, judge decisions and latency of the learned-ramp plan against the
+    plain plan (both one fbp call enqueued without a host synchronisation)."""
+    plain = S.plan_fbp(rg, ig)
+    learned = lr.plan(rg, ig)
+    geo = S.BddGeo.from_geoms(rg, ig)
+    mask = torch.as_tensor(ig.mask, device="cuda")
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    rp, rl, kept = [], [], 0
+    for i in range(n):
+        img = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(seed + i))
+        s = LF.dd_project(img, geo)
+        s = s + 0.005 * s.abs().max() * torch.randn(s.shape, device="cuda", generator=g)
+        rp.append(float(((S.fbp(plain, s) - img)[mask]).pow(2).mean().sqrt()))
+        rl.append(float(((S.fbp(learned, s) - img)[mask]).pow(2).mean().sqrt()))
+        kept += LF.fbp_learned_ramp(learned, plain, s)[1]["used"] == "learned"
+    return {"rmse_plain": float(np.mean(rp)), "rmse_learned_ramp": float(np.mean(rl)),
+            "judge_kept_learned": int(kept), "eval_scans": n,
+            "latency_ms_plain": latency(lambda: S.fbp(plain, s, sync=False)),
+            "latency_ms_learned_ramp": latency(lambda: S.fbp(learned, s, sync=False))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--phantoms", type=int, default=20000)
@@ -82,8 +108,21 @@ def main():
     ap.add_argument("--eval", type=int, default=32)
     ap.add_argument("--out", default=LF.default_weights_path())
     ap.add_argument("--eval-only", action="store_true", help="evaluate the weights at --out without training")
+    ap.add_argument("--linear", action="store_true", help="fit the learned linear (ramp) filter instead")
     args = ap.parse_args()
     rg, ig = LF.sparse_fan_geometry()
+    if args.linear:
+        out = args.out if args.out != LF.default_weights_path() else LF.default_ramp_path()
+        if args.eval_only:
+            lr = LF.LearnedRamp.load(out)
+        else:
+            t0 = time.perf_counter()
+            lr = LF.fit_learned_ramp(args.phantoms, args.seed, rg, ig)
+            lr.meta["fit_seconds"] = time.perf_counter() - t0
+            os.makedirs(os.path.dirname(out), exist_ok=True)
+            lr.save(out)
+        print(json.dumps({"weights": out, **lr.meta, **linear_summary(lr, rg, ig, args.eval)}))
+        return
     plan = S.plan_fbp(rg, ig)
     if args.eval_only:
         lf = LF.LearnedFilter.load(args.out)

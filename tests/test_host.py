@@ -175,3 +175,19 @@ def test_footprint_size_bad_dso():
         S.footprint_size(C.to_geom(g), C.to_image(dict(dims=(80, 80, 4), deltas=(1.0, 1.0, 1.0))))
     with pytest.raises(ValueError, match="bad dso"):
         O.footprint_size(g, dict(dims=(80, 80, 4), deltas=(1.0, 1.0, 1.0)))
+
+
+def test_learned_ramp_gain_file_and_round_trip(tmp_path):
+    """The committed learned-ramp gain is even (a real, symmetric row filter), passes DC and
+    only attenuates; a saved gain loads back unchanged; a gain of the wrong length is refused."""
+    from sinograms import learned as LF
+    lr = LF.LearnedRamp.load(LF.default_ramp_path())
+    g = lr.gain
+    assert g.shape == (lr.npad,) and np.array_equal(g[1:], g[1:][::-1])
+    assert abs(g[0] - 1.0) < 1e-3 and g.max() < 1.01 and g.min() > 0.0
+    p = str(tmp_path / "g.npz")
+    lr.save(p)
+    back = LF.LearnedRamp.load(p)
+    assert np.array_equal(back.gain, g) and back.npad == lr.npad and back.meta["phantoms"] == lr.meta["phantoms"]
+    with pytest.raises(S.SinogramsArgumentError):
+        LF.LearnedRamp(g[:-1], lr.npad)
