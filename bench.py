@@ -347,10 +347,10 @@ def measure_batched(args):
     t0 = time.perf_counter()
     batch = S.FDKBatch(rgs, igs)
     t_plan = time.perf_counter() - t0
+    projs = []
     for i, (rg, e) in enumerate(zip(rgs, ells)):
-        p = S.ellipsoid_proj(rg, e, device=True)
-        batch.set_input(i, p)
-        del p
+        projs.append(S.ellipsoid_proj(rg, e, device=True))
+        batch.set_input(i, projs[-1])
     st = torch.cuda.current_stream()
     for _ in range(args.warmup):
         batch.run(sync=False)
@@ -366,11 +366,20 @@ def measure_batched(args):
     ms = e0.elapsed_time(e1) / args.steps
     info = batch.info()
     stages = batch.timing()
+    # every persistent launch does its work on every run: with all inputs doubled, every scan's
+    # volume must come out exactly doubled (scaling by 2 is exact in every stage)
+    first = [batch.get_output(i, device=True) for i in range(len(rgs))]
+    for i, p in enumerate(projs):
+        batch.set_input(i, 2 * p)
+    batch.run()
+    doubled = all(bool(torch.equal(batch.get_output(i, device=True), 2 * first[i])) for i in range(len(rgs)))
+    del first, projs
     return {"workload": "fdk_batch_48_uneven_scans_seed4", "value": info["updates"] / (ms / 1e3), "unit": UNIT,
             "ms_per_run": ms, "updates_per_run": info["updates"], "scans": info["scans"],
             "work_items": info["work_items"], "persistent_ctas": info["ctas"], "persistent_launches": info["launches"],
             "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps,
-            "stage_ms": {"filters": stages[0], "back_by_box_class": stages[1:]}}
+            "stage_ms": {"filters": stages[0], "back_by_box_class": stages[1:]}, "box_classes": info["classes"],
+            "rerun_with_doubled_inputs_exact": doubled}
 
 
 def _per_call_ms(fn, reps):

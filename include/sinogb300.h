@@ -319,7 +319,9 @@ SGB_API int sgb_batch_fdk_buffers(sgb_batch *batch, int i, float **proj_dev, flo
 /* fdk of every scan (one graph launch on `stream`). */
 SGB_API int sgb_batch_fdk_run(sgb_batch *batch, int flags, void *stream);
 /* *updates = total voxel-view updates; info = {nscans, work items, persistent CTAs of the
- * first launch, number of persistent launches (one per detector-box width class)}. */
+ * first launch, number of persistent launches (one per box class)}, then, for each launch c
+ * while n >= 4 + 5 (c + 1): info[4 + 5c ..] = {box width, voxels per thread along z, bytes per
+ * box sample, views per stage, persistent CTAs}. */
 SGB_API int sgb_batch_fdk_info(const sgb_batch *batch, long long *updates, int *info, int n);
 /* Stage times of the last run (ms): [0] all weighted filters, [1..] each persistent launch. */
 SGB_API int sgb_batch_fdk_timing(sgb_batch *batch, double *ms, int n);

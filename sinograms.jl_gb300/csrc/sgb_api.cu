@@ -208,10 +208,10 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
         candidates.push_back(64 * 4 + 1);
         candidates.push_back(64 * 4 + 2);
     }
-    if (!tune) {  // batched scans: the largest ZU (64 for pair boxes, 32) whose box ring still lets two
-                  // CTAs share an SM, else 16
-        best = 16 * 4 + 1;
-        for (int zu : {64, 32}) {
+    if (!tune) {  // batched scans: the largest ZU (64 for pair boxes, 32, 16) whose box ring still lets
+                  // two CTAs share an SM.  Pair boxes that fit no ZU that way give way to plain FP32
+                  // boxes (half the bytes: the caller retries); FP32 boxes then fall back to ZU 16.
+        for (int zu : {64, 32, 16}) {
             if (zu == 64 && A.elem_bytes != 8) continue;
             FdkTmaArgs T = A;
             T.zu = zu;
@@ -221,6 +221,10 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
                 best = zu * 4 + 1;
                 break;
             }
+        }
+        if (!best) {
+            if (A.elem_bytes == 8) return SGB_OK;  // P->tma stays false
+            best = 16 * 4 + 1;
         }
     }
     if (!best) {
@@ -947,7 +951,7 @@ struct sgb_batch {
     cudaStream_t capture = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t ev[12] = {};  // graph event nodes: start, filters done, each class done
+    cudaEvent_t ev[2 + kMaxBatchClasses] = {};  // graph event nodes: start, filters done, each class done
     ~sgb_batch() {
         for (auto &e : ev)
             if (e) cudaEventDestroy(e);
@@ -988,7 +992,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         split_bytes = std::max(split_bytes, filter_scratch_bytes(P->filt, (long long)P->cg.nt * P->cg.na));
     }
     SGB_TRY(B->split.reserve(split_bytes));  // no allocation may happen during capture
-    SGB_TRY(B->counter.reserve(4 * sizeof(int)));
+    SGB_TRY(B->counter.reserve(kMaxBatchClasses * sizeof(int)));
     // per-scan tensor maps (each with its own box width) and device argument table
     std::vector<FdkTmaArgs> scans(n);
     for (int i = 0; i < n; i++) {
@@ -1030,10 +1034,20 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
             C.zu = zu;
             C.box_bytes = box_bytes;
             C.elem_bytes = elem;
-            C.vps = 4;
-            if (fdk_batch_smem(C) > 200 * 1024) C.vps = 2;
-            if (fdk_batch_smem(C) > 200 * 1024) C.vps = 1;
-            SGB_REQUIRE(fdk_batch_smem(C) <= 200 * 1024, "batch_fdk: staged boxes too large for shared memory");
+            // views per stage: the most resident CTAs per SM first (the kernel is issue-bound, so
+            // two CTAs of 9 warps beat one CTA with a deeper ring), then the most views per stage
+            int best_vps = 0, best_per = 0;
+            for (int vps : {4, 2, 1}) {
+                C.vps = vps;
+                if (fdk_batch_smem(C) > 200 * 1024) continue;
+                const int per = fdk_batch_ctas_per_sm(C);
+                if (per > best_per) {
+                    best_per = per;
+                    best_vps = vps;
+                }
+            }
+            SGB_REQUIRE(best_vps > 0, "batch_fdk: staged boxes too large for shared memory");
+            C.vps = best_vps;
             class_begin.push_back(work.size());
             for (int i : order) {
                 const FdkTmaArgs &A = scans[i];
@@ -1045,7 +1059,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         }
     }
     SGB_TRY(upload_raw(work.data(), sizeof(int2) * work.size(), B->work, st));
-    SGB_REQUIRE(B->classes.size() <= 10, "batch_fdk: more than 10 box classes");
+    SGB_REQUIRE(B->classes.size() <= (size_t)kMaxBatchClasses, "batch_fdk: more than %d box classes", kMaxBatchClasses);
     for (size_t c = 0; c < B->classes.size(); c++) {
         FdkBatchArgs &C = B->classes[c];
         C.scans = B->scans.as<FdkTmaArgs>();
@@ -1069,7 +1083,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
         sgb_plan *P = B->plans[i];
         s = run_filter(P, P->in_buf.as<float>(), (long long)P->cg.nt * P->cg.na, P->filt_buf.p, B->capture, P->pitch);
     }
-    if (s == SGB_OK && cudaMemsetAsync(B->counter.p, 0, 4 * sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
+    if (s == SGB_OK && cudaMemsetAsync(B->counter.p, 0, kMaxBatchClasses * sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
     if (s == SGB_OK && cudaEventRecordWithFlags(B->ev[1], B->capture, cudaEventRecordExternal) != cudaSuccess)
         s = SGB_ERR_CUDA;
     for (size_t c = 0; c < B->classes.size() && s == SGB_OK; c++) {
@@ -1156,6 +1170,17 @@ int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n)
     info[1] = B->args.nwork;
     info[2] = B->nctas;
     info[3] = (int)B->classes.size();
+    // per launch c (when n allows): box width, voxels per thread along z, bytes per box
+    // sample, views per stage, persistent CTAs
+    for (size_t c = 0; c < B->classes.size() && n >= 4 + 5 * (int)(c + 1); c++) {
+        const FdkBatchArgs &C = B->classes[c];
+        int *o = info + 4 + 5 * c;
+        o[0] = C.W;
+        o[1] = C.zu;
+        o[2] = C.elem_bytes;
+        o[3] = C.vps;
+        o[4] = B->class_ctas[c];
+    }
     return SGB_OK;
 }
 

@@ -29,6 +29,9 @@ struct FdkTmaArgs {
 // Batched persistent back-projection: per-scan arguments in device memory, tensor maps in
 // the kernel parameter block (at most kMaxBatch scans per launch).
 constexpr int kMaxBatch = 64;
+// persistent launches of one batch: box classes of (sample bytes 8/4/2) x (width 32/64/128) x
+// (z unroll 16/32/64) that occur, at most this many; each has its own work counter
+constexpr int kMaxBatchClasses = 10;
 struct FdkBatchMaps {
     CUtensorMap m[kMaxBatch];
 };

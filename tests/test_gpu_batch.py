@@ -37,6 +37,10 @@ def test_batch_equals_single_scan_plans(cuda, storage):
     batch = S.FDKBatch(rgs, igs, storage=storage)
     info = batch.info()
     assert info["scans"] == len(rgs) and info["ctas"] > 0
+    assert len(info["classes"]) == info["launches"] and info["classes"][0]["ctas"] == info["ctas"]
+    for c in info["classes"]:
+        assert c["box_width"] in (32, 64, 128) and c["zu"] in (16, 32, 64) and c["views_per_stage"] in (1, 2, 4)
+        assert c["sample_bytes"] in (2, 4, 8) and c["ctas"] > 0
     projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
     for i, p in enumerate(projs):
         batch.set_input(i, p)
@@ -70,3 +74,30 @@ def test_batch_rejects_too_many_scans():
     igs = [S.ImageGeom((8, 8, 4))] * 65
     with pytest.raises(S.SinogramsArgumentError):
         S.FDKBatch(rgs, igs)
+
+
+def test_batch_every_box_class_reruns_with_new_inputs(cuda):
+    """The uneven 48-scan workload (its geometry; 24 views per scan) spreads over more than
+    four persistent launches.  A second run with every input doubled must give exactly twice
+    the first run's volumes in every scan (each launch's work counter is reset per run), and
+    each scan must match its own single-scan plan."""
+    import torch
+    rgs, igs, ells = S.random_ct_scans(48, 4)
+    rgs = [type(rg)(ns=rg.ns, nt=rg.nt, ds=rg.ds, dt=rg.dt, na=24, dsd=rg.dsd, dod=rg.dod) for rg in rgs]
+    batch = S.FDKBatch(rgs, igs)
+    info = batch.info()
+    assert info["launches"] > 4, info["classes"]
+    projs = [S.ellipsoid_proj(rg, e, device=True) for rg, e in zip(rgs, ells)]
+    for i, p in enumerate(projs):
+        batch.set_input(i, p)
+    batch.run()
+    first = [batch.get_output(i) for i in range(len(rgs))]
+    for i, p in enumerate(projs):
+        batch.set_input(i, 2 * p)
+    batch.run()
+    for i in range(len(rgs)):
+        assert np.array_equal(batch.get_output(i), 2 * first[i]), i
+    for i, (rg, ig, p) in enumerate(zip(rgs, igs, projs)):
+        single = S.fdk(S.plan_fbp(rg, ig), p)
+        single = single.cpu().numpy() if isinstance(single, torch.Tensor) else single
+        assert O.rel_rmse(first[i], single) < 1e-5, i
