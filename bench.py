@@ -467,7 +467,11 @@ def measure_2d(args):
         # distance-driven projection of a 512^2 image over the scan's 90 views; FLOPs per the fixed
         # count na * nPix * (2 nPix + 7 (nDet + 1))
         img0 = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000))
-        ms_dd = _per_call_ms(lambda: LF.dd_project(img0, geo), reps)
+        dd_plan, ph0 = LF.bdd_plan(geo), LF.image_to_dd(img0)
+        sino_dd = torch.empty((geo.nDet, len(geo.angle)), device="cuda")
+        img_dd = torch.empty_like(ph0)
+        ms_dd = _per_call_ms(lambda: dd_plan.project(ph0, out=sino_dd, sync=False), reps)
+        ms_ddb = _per_call_ms(lambda: dd_plan.backproject(sino_dd, out=img_dd, sync=False), reps)
         dd_flops = float(len(geo.angle) * geo.nPix * (2 * geo.nPix + 7 * (geo.nDet + 1)))
         try:
             fp32_peak = S.measure_peaks()["fp32_flops_per_s"]
@@ -477,7 +481,9 @@ def measure_2d(args):
             "ms_plain_fbp": ms_plain, "ms_learned_fbp": ms_learned, "ms_network": ms_net,
             "network_tflops": net_flops / (ms_net / 1e3) / 1e12,
             "network_frac_of_bf16_peak": net_flops / (ms_net / 1e3) / (_peaks().get("bf16_tflops", 1941.6) * 1e12),
-            "dd_project_ms": ms_dd, "dd_project_call": "blocking (includes one stream synchronisation)",
+            "dd_project_ms": ms_dd, "dd_backproject_ms": ms_ddb,
+            "dd_project_call": "BddPlan calls on device tensors, enqueued back to back: project = output clear +"
+                               " one launch; backproject = output clear + per-view set-up + one launch",
             "dd_project_tflops": dd_flops / (ms_dd / 1e3) / 1e12,
             "dd_project_frac_of_fp32": (dd_flops / (ms_dd / 1e3) / fp32_peak) if fp32_peak else None,
             "rmse_vs_phantom_plain": float(np.mean(rp)), "rmse_vs_phantom_learned": float(np.mean(rl)),

@@ -199,6 +199,24 @@ SGB_API int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, c
                         double DSD, double DS0, double pSize, double dSize, float *image, int flags,
                         void *stream);
 
+/* No counterpart in the reference (which rebuilds its geometry on every call).  A plan of
+ * the projector pair for one geo tuple (DSD, DS0, pSize, dSize, nPix, nDet, angle): the
+ * angles and the forward projector's per-view set-up stay on the device, so
+ * sgb_bdd_plan_project is one projection launch plus the clearing of its output, with
+ * no allocation (host-pointer calls reserve plan-owned staging buffers on first use).
+ * Same layouts and results as sgb_bdd_project / sgb_bdd_backproject.  flags as for the
+ * FDK plan calls: SGB_DEVICE_PTRS for device pointers; without SGB_ASYNC the call waits
+ * for its stream.  Calls on one plan use its scratch and must be serialised on one
+ * stream. */
+typedef struct sgb_bdd_plan sgb_bdd_plan;
+SGB_API int sgb_bdd_plan_create(int nPix, int nDet, int na, const double *angle, double DSD, double DS0,
+                                double pSize, double dSize, sgb_bdd_plan **plan);
+SGB_API int sgb_bdd_plan_project(sgb_bdd_plan *plan, const float *phantom, float *sino, int flags,
+                                 void *stream);
+SGB_API int sgb_bdd_plan_backproject(sgb_bdd_plan *plan, const float *sino, float *image, int flags,
+                                     void *stream);
+SGB_API int sgb_bdd_plan_destroy(sgb_bdd_plan *plan);
+
 /* Analytic line integrals standing in for ImagePhantoms.radon(rays(rg), ob) in the
  * reference tests (test/fbp2/fbp-fan.jl:106-109, test/fbp3/fdk.jl:23), with the ray
  * geometry of rays(rg) (sino-geom.jl:368-401, ct-geom.jl:227-239).

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <vector>
 
@@ -933,6 +934,82 @@ int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, const dou
                         double DSD, double DS0, double pSize, double dSize, float *image, int flags,
                         void *stream) {
     return bdd_seam(false, sino, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, image, flags, stream);
+}
+
+// ------------------------------------------------------- distance-driven plans
+
+}  // extern "C"
+
+// Geometry of one distance-driven projector pair, kept on the device: the view angles and
+// the forward projector's per-view set-up (mapped detector boundaries, L[n]), computed once.
+// The back-projector's set-up depends on the sinogram and runs per call in the plan's scratch.
+struct sgb_bdd_plan {
+    BddArgs G{};
+    DevBuf angle, fwd, back, din, dout;
+};
+
+extern "C" {
+
+int sgb_bdd_plan_create(int nPix, int nDet, int na, const double *angle, double DSD, double DS0, double pSize,
+                        double dSize, sgb_bdd_plan **out) {
+    SGB_REQUIRE(out && angle, "bdd_plan_create: null argument");
+    SGB_REQUIRE(nPix > 0 && nDet > 0 && na > 0, "bdd_plan_create: sizes must be positive");
+    *out = nullptr;
+    auto P = std::make_unique<sgb_bdd_plan>();
+    cudaStream_t st = nullptr;
+    SGB_TRY(upload_f64(angle, na, P->angle, st));
+    P->G = BddArgs{nPix, nDet, na, P->angle.as<double>(), DSD, DS0, pSize, dSize};
+    SGB_TRY(P->fwd.reserve(bdd_project_scratch(P->G)));
+    SGB_TRY(P->back.reserve(bdd_back_scratch(P->G)));
+    SGB_TRY(launch_bdd_project_setup(P->G, P->fwd.p, st));
+    SGB_CUDA(cudaStreamSynchronize(st));
+    *out = P.release();
+    return SGB_OK;
+}
+
+int sgb_bdd_plan_project(sgb_bdd_plan *P, const float *phantom, float *sino, int flags, void *stream) {
+    SGB_REQUIRE(P && phantom && sino, "bdd_plan_project: null argument");
+    cudaStream_t st = as_stream(stream);
+    const BddArgs &G = P->G;
+    const void *in_dev;
+    SGB_TRY(stage_in(phantom, (size_t)G.nPix * G.nPix * sizeof(float), flags, P->din, &in_dev, st));
+    float *out_dev = sino;
+    const size_t nout = (size_t)G.na * G.nDet;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->dout.reserve(nout * sizeof(float)));
+        out_dev = P->dout.as<float>();
+    }
+    SGB_TRY(launch_bdd_project_main(G, static_cast<const float *>(in_dev), out_dev, P->fwd.p, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(sino, out_dev, nout * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (flags & SGB_ASYNC) return SGB_OK;
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int sgb_bdd_plan_backproject(sgb_bdd_plan *P, const float *sino, float *image, int flags, void *stream) {
+    SGB_REQUIRE(P && sino && image, "bdd_plan_backproject: null argument");
+    cudaStream_t st = as_stream(stream);
+    const BddArgs &G = P->G;
+    const void *in_dev;
+    SGB_TRY(stage_in(sino, (size_t)G.na * G.nDet * sizeof(float), flags, P->din, &in_dev, st));
+    float *out_dev = image;
+    const size_t nout = (size_t)G.nPix * G.nPix;
+    if (!(flags & SGB_DEVICE_PTRS)) {
+        SGB_TRY(P->dout.reserve(nout * sizeof(float)));
+        out_dev = P->dout.as<float>();
+    }
+    SGB_TRY(launch_bdd_back(G, static_cast<const float *>(in_dev), out_dev, P->back.p, st));
+    if (!(flags & SGB_DEVICE_PTRS))
+        SGB_CUDA(cudaMemcpyAsync(image, out_dev, nout * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (flags & SGB_ASYNC) return SGB_OK;
+    SGB_CUDA(cudaStreamSynchronize(st));
+    return SGB_OK;
+}
+
+int sgb_bdd_plan_destroy(sgb_bdd_plan *P) {
+    delete P;
+    return SGB_OK;
 }
 
 // ------------------------------------------------------------------ batched FDK

@@ -301,20 +301,36 @@ size_t bdd_back_scratch(const BddArgs &G) {
     return info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + 2 * (size_t)G.na * G.nDet);
 }
 
-int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
-                       cudaStream_t st) {
-    size_t smem = project_smem(G);
-    if (smem > 220 * 1024) {
+int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
+    if (project_smem(G) > 220 * 1024) {
         set_error("project_bdd: nPix=%d nDet=%d exceed the shared-memory tile", G.nPix, G.nDet);
         return SGB_ERR_ARG;
     }
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
     float *detm = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
     float *L = detm + (size_t)G.na * (G.nDet + 1);
-    SGB_CUDA(cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)G.na * G.nDet, st));
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L, nullptr,
                                                                                              nullptr, nullptr, nullptr);
-    SGB_TRY(after_launch("bdd_setup_kernel"));
+    return after_launch("bdd_setup_kernel");
+}
+
+int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
+                       cudaStream_t st) {
+    SGB_TRY(launch_bdd_project_setup(G, scratch, st));
+    return launch_bdd_project_main(G, phantom, sino, scratch, st);
+}
+
+int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino, const void *scratch,
+                            cudaStream_t st) {
+    const size_t smem = project_smem(G);
+    if (smem > 220 * 1024) {
+        set_error("project_bdd: nPix=%d nDet=%d exceed the shared-memory tile", G.nPix, G.nDet);
+        return SGB_ERR_ARG;
+    }
+    const ViewInfo *info = static_cast<const ViewInfo *>(scratch);
+    const float *detm = reinterpret_cast<const float *>(static_cast<const char *>(scratch) + info_bytes(G.na));
+    const float *L = detm + (size_t)G.na * (G.nDet + 1);
+    SGB_CUDA(cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)G.na * G.nDet, st));
     // rows split over CTAs so that each SM holds ~8 of them (views x row blocks)
     const int target = 8 * std::max(1, num_sms());
     int rsplit = std::max(1, std::min((G.nPix + kWarps - 1) / kWarps, (target + G.na - 1) / G.na));

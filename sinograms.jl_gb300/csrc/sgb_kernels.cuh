@@ -103,6 +103,10 @@ struct BddArgs {
 };
 // scratch sizes are returned by the *_scratch functions (bytes).
 size_t bdd_project_scratch(const BddArgs &G);
+// project_bdd split for plans: the per-view set-up (geometry only) once, the projection per call
+int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st);
+int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino, const void *scratch,
+                            cudaStream_t st);
 int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
                        cudaStream_t st);
 size_t bdd_back_scratch(const BddArgs &G);

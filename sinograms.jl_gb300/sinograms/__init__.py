@@ -5,7 +5,7 @@ Names, argument meaning and error behaviour follow the reference package
 (include/sinogb300.h).  See geom.py for the array-order convention.
 """
 from ._lib import SinogramsError, launch_count, measure_peaks
-from .bdd import BddGeo, backproject_bdd, project_bdd
+from .bdd import BddGeo, BddPlan, backproject_bdd, project_bdd
 from .filters import (SinogramsArgumentError, Window, _angle_weights, fbp_filter, fbp_ramp, fbp_sino_filter,
                       fbp_sino_weight, fbp_window, fdk_view_weight, fbp_view_weight, fdk_weight_cyl, parker_weight,
                       ramp_arc, ramp_flat)

@@ -77,6 +77,10 @@ _SIGS = {
                                         P]),
     "sgb_bdd_backproject": (c_int, [P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P, c_int,
                                     P]),
+    "sgb_bdd_plan_create": (c_int, [c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P]),
+    "sgb_bdd_plan_project": (c_int, [P, P, P, c_int, P]),
+    "sgb_bdd_plan_backproject": (c_int, [P, P, P, c_int, P]),
+    "sgb_bdd_plan_destroy": (c_int, [P]),
     "sgb_ellipse_sino": (c_int, [P, P, c_int, P, c_int, P]),
     "sgb_ellipsoid_proj": (c_int, [P, P, c_int, P, c_int, P]),
     "sgb_ellipse_image": (c_int, [P, P, c_int, c_int, P, c_int, P]),

@@ -7,12 +7,13 @@ the top) and col = x, i.e. numpy ``phantom_np[col, row]``; the sinogram is Julia
 """
 from __future__ import annotations
 
+import ctypes
 from dataclasses import dataclass
 
 import numpy as np
 
 from . import _lib
-from ._arrays import Arr, empty, f64, flags_for, ptr, stream_for
+from ._arrays import Arr, empty, f64, flags_for, plan_call, ptr, stream_for
 from .filters import SinogramsArgumentError
 from .geom import _ar, _dso
 
@@ -62,3 +63,49 @@ def backproject_bdd(sinogram, geo):
     """image = backproject_bdd(sinogram, geo), bdd_2d.jl:119-220 (numpy (nPix, nPix))."""
     n = int(_g(geo, "nPix"))
     return _run("sgb_bdd_backproject", sinogram, geo, (n, n))
+
+
+class BddPlan:
+    """The projector pair for one geo tuple with its geometry kept on the GPU
+    (sgb_bdd_plan): project / backproject give the results of project_bdd /
+    backproject_bdd.  CUDA tensors stay on the device; with sync=False a call only
+    enqueues its work on torch's current stream.  Calls on one plan share its scratch:
+    keep them on one stream."""
+
+    def __init__(self, geo):
+        self.geo = geo
+        self.nPix, self.nDet = int(_g(geo, "nPix")), int(_g(geo, "nDet"))
+        ang = f64(_g(geo, "angle"))
+        self.na = len(ang)
+        self._h = ctypes.c_void_p()
+        st = _lib.lib().sgb_bdd_plan_create(self.nPix, self.nDet, self.na, ptr(ang), float(_g(geo, "DSD")),
+                                            float(_g(geo, "DS0")), float(_g(geo, "pSize")),
+                                            float(_g(geo, "dSize")), ctypes.byref(self._h))
+        if st == _lib.SGB_ERR_ARG:
+            raise SinogramsArgumentError(_lib.last_error())
+        _lib.check(st, "bdd_plan_create")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and h.value and _lib._lib is not None:
+            _lib.lib().sgb_bdd_plan_destroy(h)
+            self._h = None
+
+    def _call(self, fn, x, out_shape, out, sync):
+        a = Arr(x)
+        y = empty(out_shape, a) if out is None else out
+        flags, st = plan_call(a.device, sync)
+        _lib.check(getattr(_lib.lib(), fn)(self._h, a.ptr, ptr(y), flags, st), fn)
+        return y
+
+    def project(self, phantom, out=None, sync: bool = True):
+        """project_bdd(phantom, geo): (nPix, nPix) -> (nDet, na)."""
+        if tuple(Arr(phantom).shape) != (self.nPix, self.nPix):
+            raise SinogramsArgumentError("phantom must be (nPix, nPix)")
+        return self._call("sgb_bdd_plan_project", phantom, (self.nDet, self.na), out, sync)
+
+    def backproject(self, sinogram, out=None, sync: bool = True):
+        """backproject_bdd(sinogram, geo): (nDet, na) -> (nPix, nPix)."""
+        if tuple(Arr(sinogram).shape) != (self.nDet, self.na):
+            raise SinogramsArgumentError("sinogram must be (nDet, na)")
+        return self._call("sgb_bdd_plan_backproject", sinogram, (self.nPix, self.nPix), out, sync)

@@ -28,7 +28,7 @@ import numpy as np
 
 from . import _lib
 from ._arrays import Arr, f64, flags_for, ptr, stream_for
-from .bdd import BddGeo
+from .bdd import BddGeo, BddPlan
 from .filters import SinogramsArgumentError
 from .geom import ImageGeom, SinoFanFlat, _rfov
 from .phantoms import random_ellipses
@@ -168,16 +168,26 @@ def image_to_dd(img):
     return torch.flip(img, dims=[0]).T.contiguous()
 
 
-def dd_project(img, geo: BddGeo):
-    """DD sinogram of an ImageGeom-order image, returned in FBP order (na, nb)."""
-    ph = image_to_dd(img)
+_BDD_PLANS: dict = {}
+
+
+def bdd_plan(geo: BddGeo) -> BddPlan:
+    """The cached projector plan of a geo tuple (the data generator and the judge project
+    many images through one geometry)."""
     ang = f64(geo.angle)
-    out = torch.empty((geo.nDet, len(ang)), dtype=torch.float32, device=img.device)
-    st = _lib.lib().sgb_bdd_project(ctypes.c_void_p(ph.data_ptr()), geo.nPix, geo.nDet, len(ang), ptr(ang), geo.DSD,
-                                    geo.DS0, geo.pSize, geo.dSize, ctypes.c_void_p(out.data_ptr()),
-                                    _lib.SGB_DEVICE_PTRS, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
-    _lib.check(st, "bdd_project")
-    return out.T.contiguous()
+    key = (float(geo.DSD), float(geo.DS0), float(geo.pSize), float(geo.dSize), int(geo.nPix), int(geo.nDet),
+           ang.tobytes())
+    plan = _BDD_PLANS.get(key)
+    if plan is None:
+        if len(_BDD_PLANS) >= 8:
+            _BDD_PLANS.clear()
+        plan = _BDD_PLANS[key] = BddPlan(geo)
+    return plan
+
+
+def dd_project(img, geo: BddGeo, sync: bool = True):
+    """DD sinogram of an ImageGeom-order image, returned in FBP order (na, nb)."""
+    return bdd_plan(geo).project(image_to_dd(img), sync=sync).T.contiguous()
 
 
 def phantom_ellipses(seed: int, n: int = 20):

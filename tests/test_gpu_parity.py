@@ -246,6 +246,28 @@ def test_gpu_bdd_adjoint_and_shapes(cuda):
     close(Aty, O.backproject_bdd(y, ogeo))
 
 
+def test_bdd_plan_matches_per_call_projector(cuda):
+    """BddPlan (geometry kept on the GPU) gives the results of project_bdd / backproject_bdd,
+    for host arrays and for device tensors with asynchronous calls.  Both run the same kernels;
+    their partial sums meet in float atomics, so the order (and the last bits) may differ."""
+    import torch
+    f, g = fix("bdd"), C.BDD
+    geo = S.BddGeo(g["DSD"], g["DS0"], g["pSize"], g["dSize"], g["nPix"], g["nDet"], g["angle"])
+    plan = S.BddPlan(geo)
+    ph, sino = f["phantom"].astype(np.float32), f["sino"].astype(np.float32)
+    ref_p, ref_b = S.project_bdd(ph, geo), S.backproject_bdd(sino, geo)
+    close(plan.project(ph), ref_p, rmse=1e-6, maxrel=1e-6)
+    close(plan.backproject(sino), ref_b, rmse=1e-6, maxrel=1e-6)
+    for _ in range(2):  # repeated calls on the plan's scratch
+        out_p = plan.project(torch.as_tensor(ph, device="cuda"), sync=False)
+        out_b = plan.backproject(torch.as_tensor(sino, device="cuda"), sync=False)
+        torch.cuda.synchronize()
+        close(out_p.cpu().numpy(), ref_p, rmse=1e-6, maxrel=1e-6)
+        close(out_b.cpu().numpy(), ref_b, rmse=1e-6, maxrel=1e-6)
+    with pytest.raises(S.SinogramsArgumentError):
+        plan.project(ph[:-1])
+
+
 # -------------------------------------------------------------- BF16 storage form
 
 def test_fdk_bf16_form_error_level(cuda):
