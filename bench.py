@@ -642,6 +642,30 @@ def run_batch_case(args):
     print(json.dumps({"case": "fdk_batch_48_uneven_scans_seed4", **batch.info(), "stage_ms": batch.timing()}))
 
 
+def run_dd_case(args):
+    """Distance-driven projector pair on the learned-filter scan (512^2 image, 888 bins, 90 views):
+    one random-ellipse phantom projected and back-projected through its BddPlan, 5 + 20 times each,
+    device tensors, calls enqueued back to back."""
+    import torch
+
+    import sinograms as S
+    from sinograms import learned as LF
+    rg, ig = LF.sparse_fan_geometry()
+    geo = S.BddGeo.from_geoms(rg, ig)
+    plan = LF.bdd_plan(geo)
+    ph = LF.image_to_dd(LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000)))
+    sino = torch.empty((geo.nDet, len(geo.angle)), device="cuda")
+    back = torch.empty_like(ph)
+    ms = {}
+    for name, fn in (("project", lambda: plan.project(ph, out=sino, sync=False)),
+                     ("backproject", lambda: plan.backproject(sino, out=back, sync=False))):
+        for _ in range(5):
+            fn()
+        ms[name] = _per_call_ms(fn, 20)
+    print(json.dumps({"case": "dd_fanflat_512x512_888x90", "ms_project": ms["project"],
+                      "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
+
+
 def run_case(args):
     """Reduced profiling case (one GPU, a few launches): fdk of 512x512x64 voxels from
     180 views of the benchmark geometry; the filtered projections (141 MB) exceed L2."""
@@ -650,6 +674,8 @@ def run_case(args):
     import sinograms as S
     if args.case == "fdk-batch":
         return run_batch_case(args)
+    if args.case == "dd-fanflat-888x90":
+        return run_dd_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -672,7 +698,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch"], help="run a profiling case instead")
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fanflat-888x90"],
+                    help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
     args = ap.parse_args()
     if args.case:

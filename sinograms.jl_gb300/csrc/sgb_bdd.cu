@@ -10,11 +10,13 @@
 // affine function of the pixel index: rowm[c] = r0 + c * delta.  The kernels use that
 // closed form instead of a table.  The interpolated prefix integral of a row at a mapped
 // point is F(q) = delta * (sum_{c<floor q} val[c] + frac(q) val[floor q]), q = (u-r0)/delta,
-// clamped to [0, nPix] (Flat extrapolation).  The reference's |diff| of F at consecutive
-// boundaries is evaluated as a local sum over the few pixels (or detector bins) between
-// them plus the two fractional end terms: exactly the same quantity, and accurate in FP32
-// because no large prefix values are subtracted.  FP64 is kept for the per-view and
-// per-row geometry (trig, boundary mapping); the per-sample work is FP32.
+// clamped to [0, nPix] (Flat extrapolation).  The forward projector takes the reference's
+// |diff| of F at consecutive detector boundaries from a warp-level prefix scan kept in
+// two-float (hi + lo) arithmetic, so nearby prefix values subtract without losing FP32
+// accuracy; the back-projector evaluates each pixel's |diff| as a local sum over the few
+// detector bins it covers plus the two fractional end terms.  Both are exactly the
+// reference's quantity.  FP64 is kept for the per-view and per-row geometry (trig,
+// boundary mapping); the per-sample work is FP32.
 //
 // Quirks kept: detector y offset -(DSD-DS0) - dSize/2 (:29), Flat extrapolation,
 // |diff| (the pair is not linear for signed images), the (na, nDet) sinogram layout,
@@ -32,6 +34,7 @@ namespace {
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kWarps = 8;
 constexpr int kThreads = 32 * kWarps;
+constexpr int kStageU = 8;  // phantom loads per thread in flight while a row block is staged
 
 struct ViewInfo {
     double rtx, rty;
@@ -144,58 +147,128 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
     }
 }
 
-// |F(hi) - F(lo)| / delta for a row: local sum of val over [lo, hi] in pixel units,
-// lo, hi clamped to [0, nPix]; val has nPix+1 entries (the last one zero).
-__device__ __forceinline__ float row_span(const float *val, int nPix, float q0, float q1) {
-    float lo = fminf(q0, q1), hi = fmaxf(q0, q1);
-    lo = fminf(fmaxf(lo, 0.f), (float)nPix);
-    hi = fminf(fmaxf(hi, 0.f), (float)nPix);
-    const int c0 = (int)lo, c1 = (int)hi;
-    float s = (hi - c1) * val[c1] - (lo - c0) * val[c0];
-    for (int c = c0; c < c1; c++) s += val[c];
-    return s;
+// Two-float accumulation (Knuth's TwoSum): (hi, lo) += v with the rounding error of the
+// high part carried in lo.
+__device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v) {
+    const float s = hi + v, bb = s - hi;
+    lo += (hi - (s - bb)) + (v - bb);
+    hi = s;
 }
 
 // ------------------------------------------------------------------ forward
+// Per view and image row: the row's prefix integral P[c] = sum_{j<c} val[j] (c = 0..nPix, in
+// pixel units) is built by a warp-level scan in two-float arithmetic, so that the difference
+// of two nearby prefix values keeps FP32 accuracy relative to the pixels between them.  The
+// interpolated integral at a mapped detector boundary is F(q) = P[c] + frac(q) val[c],
+// c = floor(q), q clamped to [0, nPix] (Flat extrapolation, val[nPix] = 0).  Lane k of the
+// warp evaluates boundary k of a group of 32 and takes F at boundary k+1 from its neighbour
+// (shuffle): neighbouring lanes read neighbouring pixels (no bank conflicts), each boundary
+// is evaluated once, and each bin is |F(k+1) - F(k)| (:98-101).
 __global__ void __launch_bounds__(kThreads)
     bdd_project_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L,
                        const float *__restrict__ phantom, float *sino, int rows_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet, p = blockIdx.x;
-    float *dm = reinterpret_cast<float *>(smraw);   // nDet+1
-    float *tile = dm + (nDet + 1);                    // kWarps x (nPix+1)
-    float *accw = tile + kWarps * (nPix + 1);         // kWarps x nDet
+    float2 *pw = reinterpret_cast<float2 *>(smraw);                   // kWarps x (nPix+1): prefix (hi, lo)
+    float *vw = reinterpret_cast<float *>(pw + kWarps * (nPix + 1));  // kWarps x (nPix+1): row values
+    float *dm = vw + kWarps * (nPix + 1);                              // nDet+1
+    float *accw = dm + (nDet + 1);                                     // kWarps x nDet
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
     const ViewInfo vi = info[p];
     for (int k = threadIdx.x; k <= nDet; k += kThreads) dm[k] = detm[(size_t)p * (nDet + 1) + k];
     for (int i = threadIdx.x; i < kWarps * nDet; i += kThreads) accw[i] = 0.f;
-    float *val = tile + warp * (nPix + 1);
+    float2 *pre = pw + warp * (nPix + 1);
+    float *val = vw + warp * (nPix + 1);
     float *acc = accw + warp * nDet;
+    const int chunk = ((nPix + 1 + 31) / 32) | 1;  // prefix entries per lane (odd: conflict-free reads)
+    const int c_begin = min(nPix + 1, lane * chunk), c_end = min(nPix + 1, c_begin + chunk);
     const int r_begin = blockIdx.y * rows_per_cta, r_end = min(nPix, r_begin + rows_per_cta);
     for (int rb = r_begin; rb < r_end; rb += kWarps) {
         __syncthreads();
-        // stage kWarps rows: x-case row r = phantom[r + nPix*c]; y-case (transposed and
-        // reversed, :67) row r = phantom[(nPix-1-c) + nPix*r]; val[nPix] = 0
-        for (int i = threadIdx.x; i < kWarps * (nPix + 1); i += kThreads) {
-            int w, c;
-            if (vi.axis) { w = i % kWarps; c = i / kWarps; }
-            else { w = i / (nPix + 1); c = i % (nPix + 1); }
-            int r = rb + w;
-            float v = 0.f;
-            if (r < r_end && c < nPix)
-                v = vi.axis ? __ldg(phantom + r + (size_t)nPix * c)
-                            : __ldg(phantom + (nPix - 1 - c) + (size_t)nPix * r);
-            tile[w * (nPix + 1) + c] = v;
+        // stage kWarps rows: x-case row r = phantom[r + nPix*c] (eight consecutive r per 32-byte
+        // sector); y-case (transposed and reversed, :67) row r = phantom[(nPix-1-c) + nPix*r]
+        // (kStageU independent loads in flight per thread before their stores)
+        if (vi.axis) {
+            const int total = kWarps * nPix;
+            for (int i0 = threadIdx.x; i0 < total; i0 += kStageU * kThreads) {
+                float v[kStageU];
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int i = i0 + u * kThreads, r = rb + i % kWarps;
+                    v[u] = (i < total && r < r_end) ? __ldg(phantom + r + (size_t)nPix * (i / kWarps)) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int i = i0 + u * kThreads;
+                    if (i < total) vw[(i % kWarps) * (nPix + 1) + i / kWarps] = v[u];
+                }
+            }
+        } else {
+            const int r = rb + warp;
+            const float *src = phantom + (size_t)nPix * r + (nPix - 1);
+            for (int c0 = lane; c0 < nPix; c0 += kStageU * 32) {
+                float v[kStageU];
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int c = c0 + 32 * u;
+                    v[u] = (c < nPix && r < r_end) ? __ldg(src - c) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kStageU; u++)
+                    if (c0 + 32 * u < nPix) val[c0 + 32 * u] = v[u];
+            }
         }
+        if (threadIdx.x < kWarps) vw[threadIdx.x * (nPix + 1) + nPix] = 0.f;
         __syncthreads();
         const int r = rb + warp;
-        if (r >= r_end) continue;
+        if (r >= r_end) continue;  // warp-uniform
+        // prefix: lane totals, warp scan of the totals, then the lane's entries
+        float th = 0.f, tl = 0.f;
+        for (int c = c_begin; c < c_end; c++) two_sum_add(th, tl, val[c]);
+        for (int off = 1; off < 32; off <<= 1) {
+            const float oh = __shfl_up_sync(full, th, off), ol = __shfl_up_sync(full, tl, off);
+            if (lane >= off) {
+                two_sum_add(th, tl, oh);
+                tl += ol;
+            }
+        }
+        float sh = __shfl_up_sync(full, th, 1), sl = __shfl_up_sync(full, tl, 1);
+        if (lane == 0) sh = sl = 0.f;
+        for (int c = c_begin; c < c_end; c++) {
+            pre[c] = make_float2(sh, sl);
+            two_sum_add(sh, sl, val[c]);
+        }
+        __syncwarp();
         double r0d, deltad;
         row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
         const float r0 = (float)r0d, rdelta = (float)(1.0 / deltad), adelta = (float)std::fabs(deltad);
-        for (int n = lane; n < nDet; n += 32) {
-            const float q0 = (dm[n] - r0) * rdelta, q1 = (dm[n + 1] - r0) * rdelta;
-            acc[n] += fabsf(row_span(val, nPix, q0, q1)) * adelta;  // |diff(Pdk)|, :101
+        const float qmax = (float)nPix;
+        // F at mapped detector boundary k (:98, interpolation of the row's prefix integral);
+        // floor(q) for 0 <= q <= nPix < 2^22 by the round-down add of 2^23 (no conversions)
+        auto F = [&](int k, float &fh, float &fl) {
+            const float q = fminf(fmaxf((dm[k] - r0) * rdelta, 0.f), qmax);
+            const float m = __fadd_rd(q, 8388608.f);
+            const int c = __float_as_int(m) - 0x4B000000;
+            const float2 e = pre[c];
+            fh = e.x;
+            fl = fmaf(q - (m - 8388608.f), val[c], e.y);
+        };
+        // bin k0 + lane: |F(k+1) - F(k)| * |delta| (:98-101), F(k+1) from the next lane
+        float ch, cl;
+        F(min(lane, nDet), ch, cl);
+        for (int k0 = 0; k0 < nDet; k0 += 32) {
+            float nh, nl;
+            F(min(k0 + 32 + lane, nDet), nh, nl);
+            float uh = __shfl_down_sync(full, ch, 1), ul = __shfl_down_sync(full, cl, 1);
+            const float h0 = __shfl_sync(full, nh, 0), l0 = __shfl_sync(full, nl, 0);
+            if (lane == 31) {
+                uh = h0;
+                ul = l0;
+            }
+            if (k0 + lane < nDet) acc[k0 + lane] += fabsf((uh - ch) + (ul - cl)) * adelta;
+            ch = nh;
+            cl = nl;
         }
         __syncwarp();
     }
@@ -285,7 +358,8 @@ __global__ void __launch_bounds__(kThreads)
 size_t info_bytes(int na) { return ((size_t)na * sizeof(ViewInfo) + 255) & ~(size_t)255; }
 
 size_t project_smem(const BddArgs &G) {
-    return sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * (G.nPix + 1) + (size_t)kWarps * G.nDet);
+    return (sizeof(float2) + sizeof(float)) * (size_t)kWarps * (G.nPix + 1) +
+           sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * G.nDet);
 }
 size_t back_smem(const BddArgs &G) {
     return sizeof(float) * ((size_t)(G.nDet + 1) + 2 * (size_t)G.nDet + 2 * (size_t)kWarps * G.nPix);
