@@ -379,6 +379,8 @@ def measure_batched(args):
             "work_items": info["work_items"], "persistent_ctas": info["ctas"], "persistent_launches": info["launches"],
             "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps,
             "stage_ms": {"filters": stages[0], "back_by_box_class": stages[1:]}, "box_classes": info["classes"],
+            "back_updates_per_s_by_class": [c["mupdates"] * 1e6 / (t / 1e3) if t > 0 else None
+                                            for c, t in zip(info["classes"], stages[1:])],
             "rerun_with_doubled_inputs_exact": doubled}
 
 

@@ -1021,6 +1021,7 @@ struct sgb_batch {
     DevBuf scans, work, counter, flags, split;
     std::vector<FdkBatchArgs> classes;  // one persistent launch per box-width class
     std::vector<int> class_ctas;
+    std::vector<long long> class_updates;  // voxel-view updates of each launch
     FdkBatchArgs args{};                // totals for sgb_batch_fdk_info
     FdkBatchMaps maps;
     long long updates = 0;
@@ -1126,11 +1127,14 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
             SGB_REQUIRE(best_vps > 0, "batch_fdk: staged boxes too large for shared memory");
             C.vps = best_vps;
             class_begin.push_back(work.size());
+            long long cu = 0;
             for (int i : order) {
                 const FdkTmaArgs &A = scans[i];
                 const int ntiles = floor_div_up(A.nx, 16) * floor_div_up(A.ny, 16) * floor_div_up(A.nz, A.zu);
                 for (int t = 0; t < ntiles; t++) work.push_back(make_int2(i, t));
+                cu += (long long)A.nx * A.ny * A.nz * A.nv;
             }
+            B->class_updates.push_back(cu);
             C.nwork = (int)(work.size() - class_begin.back());
             B->classes.push_back(C);
         }
@@ -1248,15 +1252,16 @@ int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n)
     info[2] = B->nctas;
     info[3] = (int)B->classes.size();
     // per launch c (when n allows): box width, voxels per thread along z, bytes per box
-    // sample, views per stage, persistent CTAs
-    for (size_t c = 0; c < B->classes.size() && n >= 4 + 5 * (int)(c + 1); c++) {
+    // sample, views per stage, persistent CTAs, voxel-view updates in millions
+    for (size_t c = 0; c < B->classes.size() && n >= 4 + 6 * (int)(c + 1); c++) {
         const FdkBatchArgs &C = B->classes[c];
-        int *o = info + 4 + 5 * c;
+        int *o = info + 4 + 6 * c;
         o[0] = C.W;
         o[1] = C.zu;
         o[2] = C.elem_bytes;
         o[3] = C.vps;
         o[4] = B->class_ctas[c];
+        o[5] = (int)((B->class_updates[c] + 500000) / 1000000);
     }
     return SGB_OK;
 }

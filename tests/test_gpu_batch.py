@@ -40,7 +40,8 @@ def test_batch_equals_single_scan_plans(cuda, storage):
     assert len(info["classes"]) == info["launches"] and info["classes"][0]["ctas"] == info["ctas"]
     for c in info["classes"]:
         assert c["box_width"] in (32, 64, 128) and c["zu"] in (16, 32, 64) and c["views_per_stage"] in (1, 2, 4)
-        assert c["sample_bytes"] in (2, 4, 8) and c["ctas"] > 0
+        assert c["sample_bytes"] in (2, 4, 8) and c["ctas"] > 0 and c["mupdates"] >= 0
+    assert abs(sum(c["mupdates"] for c in info["classes"]) * 1e6 - info["updates"]) <= 0.5e6 * len(info["classes"])
     projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
     for i, p in enumerate(projs):
         batch.set_input(i, p)
