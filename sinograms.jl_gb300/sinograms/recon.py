@@ -11,7 +11,7 @@ import numpy as np
 
 from . import _lib
 from ._arrays import Arr, empty, f64, flags_for, plan_call, ptr, stream_for, torch
-from .filters import SinogramsArgumentError, Window, fbp_filter, fdk_view_weight, fbp_view_weight
+from .filters import SinogramsArgumentError, Window, fbp_view_weight, fdk_view_weight
 from .geom import CtFan, ImageGeom, SinoPar, _ar, _dso, _rfov, c_struct, dims, is_ct
 
 
