@@ -399,6 +399,23 @@ def _per_call_ms(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
+def _accuracy_2d(out, g, igd, sino, window, rfov):
+    """Relative RMSE and max error of a 2D FBP against the FP64 oracle on the same FP32
+    sinogram: over the FOV disk less 1 mm (the image corners meet the detector edge, where FP32
+    and FP64 rounding decide the whole-tap rule differently) and over the whole image."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    ref = O.fbp(g, igd, sino, shape=window)
+    nx, ny = igd["dims"]
+    dx, dy = igd["deltas"]
+    x = dx * (np.arange(nx) - (nx - 1) / 2)
+    y = dy * (np.arange(ny) - (ny - 1) / 2)
+    inside = (x[None, :] ** 2 + y[:, None] ** 2) <= (rfov - 1.0) ** 2
+    return {"rel_rmse_fov": O.rel_rmse(out[inside], ref[inside]),
+            "max_abs_err_rel_fov": float(np.abs(out - ref)[inside].max() / np.abs(ref).max()),
+            "rel_rmse_image": O.rel_rmse(out, ref), "oracle": "FP64 C restatement, same FP32 sinogram"}
+
+
 def measure_2d(args):
     """The 2D workloads beside the headline, device-resident, on seeded synthetic inputs:
     SinoPar 256 x 180 -> 256^2 with a Hann window; SinoFanArc 888 x 512 views over a short scan ->
@@ -423,6 +440,11 @@ def measure_2d(args):
         plan.set_timing(False)
         out["par_256x180_hann"] = {"ms_per_fbp": ms, "filter_ms": f_ms, "back_ms": b_ms,
                                    "back_updates_per_s": 256 * 256 * 180 / (b_ms / 1e3)}
+        if not args.no_cpu:
+            g = dict(kind="par", nb=256, d=1.0, offset=0.0, na=180, orbit=180.0, orbit_start=0.0)
+            out["par_256x180_hann"]["accuracy_vs_fp64"] = _accuracy_2d(
+                S.fbp(plan, sino).cpu().numpy(), g, dict(dims=(256, 256), deltas=(1.0, 1.0)),
+                sino.cpu().numpy(), "hann", S._rfov(rg))
         base = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=2, orbit=360.0)
         orbit = 180.0 + 2.0 * float(np.degrees(S._gamma_max(base)))  # short scan: 180 deg + fan angle
         rg = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=512, orbit=orbit)
@@ -437,6 +459,12 @@ def measure_2d(args):
         plan.set_timing(False)
         out["arc_888x512_short_scan"] = {"ms_per_fbp": ms, "filter_ms": f_ms, "back_ms": b_ms,
                                          "back_updates_per_s": 512 * 512 * 512 / (b_ms / 1e3)}
+        if not args.no_cpu:
+            g = dict(kind="arc", nb=888, d=1.0239, offset=0.0, dsd=949.075, dod=408.075, source_offset=0.0,
+                     orbit_start=0.0, na=512, orbit=orbit)
+            out["arc_888x512_short_scan"]["accuracy_vs_fp64"] = _accuracy_2d(
+                S.fbp(plan, sino).cpu().numpy(), g, dict(dims=(512, 512), deltas=(0.9766, 0.9766)),
+                sino.cpu().numpy(), "none", S._rfov(rg))
         rg, ig = LF.sparse_fan_geometry()
         plan = S.plan_fbp(rg, ig)
         lf = LF.LearnedFilter.load(LF.default_weights_path())
