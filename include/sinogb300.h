@@ -338,8 +338,9 @@ SGB_API int sgb_batch_fdk_buffers(sgb_batch *batch, int i, float **proj_dev, flo
 SGB_API int sgb_batch_fdk_run(sgb_batch *batch, int flags, void *stream);
 /* *updates = total voxel-view updates; info = {nscans, work items, persistent CTAs of the
  * first launch, number of persistent launches (one per box class)}, then, for each launch c
- * while n >= 4 + 6 (c + 1): info[4 + 6c ..] = {box width, voxels per thread along z, bytes per
- * box sample, views per stage, persistent CTAs, voxel-view updates in millions}. */
+ * while n >= 4 + 7 (c + 1): info[4 + 7c ..] = {box width, voxels per thread along z, bytes per
+ * box sample, views per stage, persistent CTAs, voxel-view updates in millions, stages of the
+ * box ring}. */
 SGB_API int sgb_batch_fdk_info(const sgb_batch *batch, long long *updates, int *info, int n);
 /* Stage times of the last run (ms): [0] all weighted filters, [1..] each persistent launch. */
 SGB_API int sgb_batch_fdk_timing(sgb_batch *batch, double *ms, int n);

@@ -209,9 +209,10 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
         candidates.push_back(64 * 4 + 1);
         candidates.push_back(64 * 4 + 2);
     }
-    if (!tune) {  // batched scans: the largest ZU (64 for pair boxes, 32, 16) whose box ring still lets
-                  // two CTAs share an SM.  Pair boxes that fit no ZU that way give way to plain FP32
-                  // boxes (half the bytes: the caller retries); FP32 boxes then fall back to ZU 16.
+    if (!tune) {  // batched scans: the largest ZU (64 for pair boxes, 32, 16) whose 4-stage box ring
+                  // still lets two CTAs share an SM, else ZU 64/32 with a 2-stage ring.  Pair boxes
+                  // that fit none of these give way to plain FP32 boxes (half the bytes: the caller
+                  // retries); FP32 boxes then fall back to ZU 16.
         for (int zu : {64, 32, 16}) {
             if (zu == 64 && A.elem_bytes != 8) continue;
             FdkTmaArgs T = A;
@@ -221,6 +222,23 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
             if (fdk_tma_choose(T) && fdk_tma_fits_two_ctas(T)) {
                 best = zu * 4 + 1;
                 break;
+            }
+        }
+        // Scans left at ZU 16 (or without a fit): a 2-stage ring of one view per stage at ZU 64/32
+        // still lets two CTAs share an SM, and the longer z-runs amortise the per-column set-up
+        // (measured on the 48-scan workload: 90 -> 74 ms for the largest such launch)
+        if (!best || best / 4 == 16) {
+            for (int zu : {64, 32}) {
+                if (zu == 64 && A.elem_bytes != 8) continue;
+                FdkTmaArgs T = A;
+                T.zu = zu;
+                T.passes = 1;
+                SGB_TRY(fdk_tma_prepare(T, P->flags.as<int>(), st));
+                if (fdk_tma_choose(T) && fdk_tma_fits_two_ctas_ring(T, 2)) {
+                    best = zu * 4 + 1;
+                    A.nstage = 2;
+                    break;
+                }
             }
         }
         if (!best) {
@@ -320,6 +338,7 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     A.v0 = 0;
     A.accum = 0;
     A.passes = 1;
+    A.nstage = kNStageDefault;
     A.elem_bytes = elem;
     A.err = P->flags.as<int>() + 2;
     // voxels must stay well inside the source circle for the corner bound to hold
@@ -1094,12 +1113,12 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::vector<size_t> class_begin;
     for (int ecls : {8, 4, 2}) {  // element size: FP32 pairs, FP32, BF16
-        for (int cls = 0; cls < 9; cls++) {  // box width 32/64/128 x voxels per thread along z 16/32/64
-            const int W = 32 << (cls % 3), zu = 16 << (cls / 3);
+        for (int cls = 0; cls < 18; cls++) {  // box width 32/64/128 x ZU 16/32/64 x ring of 4 or 2 stages
+            const int W = 32 << (cls % 3), zu = 16 << ((cls / 3) % 3), ns = cls < 9 ? kNStageDefault : 2;
             std::vector<int> order;
             int box_bytes = 0;
             for (int i = 0; i < n; i++)
-                if (scans[i].W == W && scans[i].elem_bytes == ecls && scans[i].zu == zu) {
+                if (scans[i].W == W && scans[i].elem_bytes == ecls && scans[i].zu == zu && scans[i].nstage == ns) {
                     order.push_back(i);
                     box_bytes = std::max(box_bytes, scans[i].box_bytes);
                 }
@@ -1112,10 +1131,13 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
             C.zu = zu;
             C.box_bytes = box_bytes;
             C.elem_bytes = elem;
+            C.nstage = ns;
             // views per stage: the most resident CTAs per SM first (the kernel is issue-bound, so
-            // two CTAs of 9 warps beat one CTA with a deeper ring), then the most views per stage
+            // two CTAs of 9 warps beat one CTA with a deeper ring), then the most views per stage;
+            // a 2-stage ring holds one view per stage
             int best_vps = 0, best_per = 0;
             for (int vps : {4, 2, 1}) {
+                if (ns == 2 && vps != 1) continue;
                 C.vps = vps;
                 if (fdk_batch_smem(C) > 200 * 1024) continue;
                 const int per = fdk_batch_ctas_per_sm(C);
@@ -1252,16 +1274,17 @@ int sgb_batch_fdk_info(const sgb_batch *B, long long *updates, int *info, int n)
     info[2] = B->nctas;
     info[3] = (int)B->classes.size();
     // per launch c (when n allows): box width, voxels per thread along z, bytes per box
-    // sample, views per stage, persistent CTAs, voxel-view updates in millions
-    for (size_t c = 0; c < B->classes.size() && n >= 4 + 6 * (int)(c + 1); c++) {
+    // sample, views per stage, persistent CTAs, voxel-view updates in millions, ring stages
+    for (size_t c = 0; c < B->classes.size() && n >= 4 + 7 * (int)(c + 1); c++) {
         const FdkBatchArgs &C = B->classes[c];
-        int *o = info + 4 + 6 * c;
+        int *o = info + 4 + 7 * c;
         o[0] = C.W;
         o[1] = C.zu;
         o[2] = C.elem_bytes;
         o[3] = C.vps;
         o[4] = B->class_ctas[c];
         o[5] = (int)((B->class_updates[c] + 500000) / 1000000);
+        o[6] = C.nstage;
     }
     return SGB_OK;
 }

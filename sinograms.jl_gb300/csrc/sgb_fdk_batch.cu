@@ -7,8 +7,9 @@ namespace sgb {
 using fdkdev::kNStage;
 
 size_t fdk_batch_smem(const FdkBatchArgs &B) {
-    return 128 + (size_t)kNStage * B.vps * B.box_bytes + (sizeof(int2) + sizeof(float2) + sizeof(float)) * kNStage * B.vps +
-           sizeof(int2) * kNStage + 2 * sizeof(uint64_t) * kNStage;
+    const int ns = B.nstage;
+    return 128 + (size_t)ns * B.vps * B.box_bytes + (sizeof(int2) + sizeof(float2) + sizeof(float)) * ns * B.vps +
+           sizeof(int2) * ns + 2 * sizeof(uint64_t) * ns;
 }
 
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B) {

@@ -179,15 +179,17 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// views per stage 4, 2 or 1 in a kNStage ring; a 2-stage ring (tall boxes) with one view per stage
 template <typename TP, int ZU, int BW>
-auto batch_kernel_for(int vps) {
+auto batch_kernel_for(int vps, int nstage) {
+    if (nstage == 2) return fdk_tma_batch_kernel<TP, ZU, BW, 1, 2>;
     return vps == 4 ? fdk_tma_batch_kernel<TP, ZU, BW, 4, kNStage>
                     : (vps == 2 ? fdk_tma_batch_kernel<TP, ZU, BW, 2, kNStage> : fdk_tma_batch_kernel<TP, ZU, BW, 1, kNStage>);
 }
 
 template <typename TP, int ZU, int BW>
 int launch_batch_t(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
-    auto k = batch_kernel_for<TP, ZU, BW>(B.vps);
+    auto k = batch_kernel_for<TP, ZU, BW>(B.vps, B.nstage);
     const size_t smem = fdk_batch_smem(B);
     SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<nctas, kThreads, smem, st>>>(B, maps);
@@ -196,9 +198,9 @@ int launch_batch_t(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, c
 
 template <typename TP, int BW>
 int batch_occupancy_w(const FdkBatchArgs &B) {
-    auto k = B.zu == 32 ? batch_kernel_for<TP, 32, BW>(B.vps) : batch_kernel_for<TP, 16, BW>(B.vps);
+    auto k = B.zu == 32 ? batch_kernel_for<TP, 32, BW>(B.vps, B.nstage) : batch_kernel_for<TP, 16, BW>(B.vps, B.nstage);
     if constexpr (sizeof(TP) == 8)
-        if (B.zu == 64) k = batch_kernel_for<TP, 64, BW>(B.vps);
+        if (B.zu == 64) k = batch_kernel_for<TP, 64, BW>(B.vps, B.nstage);
     const size_t smem = fdk_batch_smem(B);
     int n = 0;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return 0;

@@ -96,6 +96,9 @@ bool fdk_tma_choose(FdkTmaArgs &A) {
 }
 
 bool fdk_tma_fits_two_ctas(const FdkTmaArgs &A) { return A.vps && fdk_tma_smem(A, A.vps, kNStage) <= 112 * 1024; }
+bool fdk_tma_fits_two_ctas_ring(const FdkTmaArgs &A, int nstage) {
+    return fdk_tma_smem(A, 1, nstage) + sizeof(int2) * nstage <= 112 * 1024;
+}
 
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map) {
     PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();

@@ -24,6 +24,7 @@ struct FdkTmaArgs {
     int v0;                 // first view of this launch (views v0 .. v0 + nv - 1)
     int accum;              // 1: add to the volume (a later pass over views), 0: overwrite
     int passes;             // launches the views are split over (chosen by the plan's autotuner)
+    int nstage;             // batched scans: stages of the box ring (4, or 2 for tall boxes)
 };
 
 // Batched persistent back-projection: per-scan arguments in device memory, tensor maps in
@@ -31,7 +32,10 @@ struct FdkTmaArgs {
 constexpr int kMaxBatch = 64;
 // persistent launches of one batch: box classes of (sample bytes 8/4/2) x (width 32/64/128) x
 // (z unroll 16/32/64) that occur, at most this many; each has its own work counter
-constexpr int kMaxBatchClasses = 10;
+constexpr int kMaxBatchClasses = 16;
+// stages of the box ring of the TMA-staged back-projectors (batched scans with tall boxes may
+// take a 2-stage ring instead)
+constexpr int kNStageDefault = 4;
 struct FdkBatchMaps {
     CUtensorMap m[kMaxBatch];
 };
@@ -46,6 +50,7 @@ struct FdkBatchArgs {
     int elem_bytes;
     int vps;                  // views per pipeline stage (4, 2 or 1)
     int zu;                   // voxels per thread along z of every scan in the launch (16, 32, 64)
+    int nstage;               // stages of the box ring (4; 2 with one view per stage)
 };
 size_t fdk_batch_smem(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm(const FdkBatchArgs &B);
@@ -64,6 +69,8 @@ int fdk_tma_prepare(FdkTmaArgs &A, int *ext_dev, cudaStream_t st);
 bool fdk_tma_choose(FdkTmaArgs &A);
 // The chosen ring leaves room for two CTAs per SM.
 bool fdk_tma_fits_two_ctas(const FdkTmaArgs &A);
+// one view per stage in a ring of `nstage` stages lets two CTAs share an SM
+bool fdk_tma_fits_two_ctas_ring(const FdkTmaArgs &A, int nstage);
 size_t fdk_tma_smem(const FdkTmaArgs &A, int vps, int nstage);
 // 3D tensor map over the filtered projections (pitch, nt, na).
 int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap *map);

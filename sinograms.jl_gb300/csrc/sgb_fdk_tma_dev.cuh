@@ -16,7 +16,7 @@ using namespace dev;
 constexpr int kTX = 16, kTY = 16;             // columns per CTA
 constexpr int kConsumers = kTX * kTY;          // 8 consumer warps
 constexpr int kThreads = kConsumers + 32;      // + 1 producer warp
-constexpr int kNStage = 4;                     // stages in the ring (views per stage: 4, 2 or 1)
+constexpr int kNStage = kNStageDefault;        // stages in the ring (views per stage: 4, 2 or 1)
 // TMA x coordinate per box sample: pair boxes (y, dy) are two FP32 elements per sample
 template <typename TP> constexpr int kXS = sizeof(TP) == 8 ? 2 : 1;
 

@@ -302,11 +302,12 @@ class FDKBatch:
 
     def info(self) -> dict:
         """Totals, and per persistent launch its box class: box width, voxels per thread along
-        z, bytes per box sample, views per stage, persistent CTAs and updates (millions)."""
+        z, bytes per box sample, views per stage, persistent CTAs, updates (millions) and ring
+        stages."""
         u = ctypes.c_longlong()
-        a = np.zeros(4 + 6 * 10, dtype=np.int32)
+        a = np.zeros(4 + 7 * 16, dtype=np.int32)
         _status(_lib.lib().sgb_batch_fdk_info(self._h, ctypes.byref(u), ptr(a), len(a)), "batch_fdk_info")
-        keys = ("box_width", "zu", "sample_bytes", "views_per_stage", "ctas", "mupdates")
-        classes = [dict(zip(keys, (int(v) for v in a[4 + 6 * c:10 + 6 * c]))) for c in range(int(a[3]))]
+        keys = ("box_width", "zu", "sample_bytes", "views_per_stage", "ctas", "mupdates", "stages")
+        classes = [dict(zip(keys, (int(v) for v in a[4 + 7 * c:11 + 7 * c]))) for c in range(int(a[3]))]
         return dict(updates=int(u.value), scans=int(a[0]), work_items=int(a[1]), ctas=int(a[2]), launches=int(a[3]),
                     classes=classes)

@@ -40,7 +40,7 @@ def test_batch_equals_single_scan_plans(cuda, storage):
     assert len(info["classes"]) == info["launches"] and info["classes"][0]["ctas"] == info["ctas"]
     for c in info["classes"]:
         assert c["box_width"] in (32, 64, 128) and c["zu"] in (16, 32, 64) and c["views_per_stage"] in (1, 2, 4)
-        assert c["sample_bytes"] in (2, 4, 8) and c["ctas"] > 0 and c["mupdates"] >= 0
+        assert c["sample_bytes"] in (2, 4, 8) and c["ctas"] > 0 and c["mupdates"] >= 0 and c["stages"] in (2, 4)
     assert abs(sum(c["mupdates"] for c in info["classes"]) * 1e6 - info["updates"]) <= 0.5e6 * len(info["classes"])
     projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
     for i, p in enumerate(projs):
@@ -80,8 +80,8 @@ def test_batch_rejects_too_many_scans():
 def test_batch_every_box_class_reruns_with_new_inputs(cuda):
     """The uneven 48-scan workload (its geometry; 24 views per scan) spreads over more than
     four persistent launches.  A second run with every input doubled must give exactly twice
-    the first run's volumes in every scan (each launch's work counter is reset per run), and
-    each scan must match its own single-scan plan."""
+    the first run's volumes in every scan (each launch's work counter is reset per run), each
+    scan must match its own single-scan plan, and the FP64 oracle bounds both."""
     import torch
     rgs, igs, ells = S.random_ct_scans(48, 4)
     rgs = [type(rg)(ns=rg.ns, nt=rg.nt, ds=rg.ds, dt=rg.dt, na=24, dsd=rg.dsd, dod=rg.dod) for rg in rgs]
@@ -98,7 +98,23 @@ def test_batch_every_box_class_reruns_with_new_inputs(cuda):
     batch.run()
     for i in range(len(rgs)):
         assert np.array_equal(batch.get_output(i), 2 * first[i]), i
+    # Batch and single-scan plans may pick different z-unrolls (the batch keeps two CTAs per SM,
+    # the single plan is autotuned); the t coordinate bt = bt0 + k dbt is then rounded from a
+    # different base, which moves taps by ~1e-5 row on these coarse, 24-view scans.  So the
+    # volumes agree to 5e-5, and the scan that differs most is checked against the FP64 oracle
+    # on a central 4-slice slab, where both must meet the FP32 bar.
+    diffs = []
     for i, (rg, ig, p) in enumerate(zip(rgs, igs, projs)):
-        single = S.fdk(S.plan_fbp(rg, ig), p)
-        single = single.cpu().numpy() if isinstance(single, torch.Tensor) else single
-        assert O.rel_rmse(first[i], single) < 1e-5, i
+        single = S.fdk(S.plan_fbp(rg, ig), p).cpu().numpy()
+        diffs.append(O.rel_rmse(first[i], single))
+        assert diffs[-1] < 5e-5, (i, diffs[-1])
+    i = int(np.argmax(diffs))
+    rg, ig, p = rgs[i], igs[i], projs[i]
+    single = S.fdk(S.plan_fbp(rg, ig), p).cpu().numpy()
+    nz, m = ig.dims[2], 4
+    z0 = (nz - m) // 2
+    slab = dict(dims=(ig.dims[0], ig.dims[1], m), deltas=ig.deltas,
+                offsets=(0.0, 0.0, (nz - 1) / 2 - (m - 1) / 2 - z0))
+    ref = O.fdk(_oracle_geom(rg), slab, p.cpu().numpy())
+    assert O.rel_rmse(first[i][z0:z0 + m], ref) < 1e-4, (i, diffs[i])
+    assert O.rel_rmse(single[z0:z0 + m], ref) < 1e-4, (i, diffs[i])
