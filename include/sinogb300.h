@@ -178,7 +178,10 @@ SGB_API int sgb_fbp_back_fan(float *image, const float *sino, int nb, int na, co
                      double ds, float offset, const double *xc, const double *yc, int nx, int ny,
                      const uint8_t *mask, int ia_skip, int flags, void *stream);
 
-/* project_bdd, src/sys2/bdd_2d.jl:17-110: phantom (nPix,nPix) -> sino (na, nDet). */
+/* project_bdd, src/sys2/bdd_2d.jl:17-110: phantom (nPix,nPix) -> sino (na, nDet).  The
+ * projection keeps eight image rows (12 bytes per pixel) and eight bin rows per thread block in
+ * shared memory: 96 (nPix + 1) + 36 nDet + 4 <= 225280 bytes (nPix <= 2012 at nDet = 888);
+ * larger sizes return SGB_ERR_ARG. */
 SGB_API int sgb_bdd_project(const float *phantom, int nPix, int nDet, int na, const double *angle,
                     double DSD, double DS0, double pSize, double dSize, float *sino, int flags,
                     void *stream);

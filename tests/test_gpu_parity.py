@@ -268,6 +268,14 @@ def test_bdd_plan_matches_per_call_projector(cuda):
         plan.project(ph[:-1])
 
 
+def test_bdd_oversized_image_is_an_argument_error(cuda):
+    """The projection's shared-memory tiles bound nPix (2012 at nDet = 888): a larger image is
+    refused with an argument error before any launch."""
+    geo = S.BddGeo(949.0, 541.0, 0.25, 1.0239, 2100, 888, np.linspace(0, 2 * np.pi, 8, endpoint=False))
+    with pytest.raises(S.SinogramsArgumentError):
+        S.BddPlan(geo)
+
+
 # -------------------------------------------------------------- BF16 storage form
 
 def test_fdk_bf16_form_error_level(cuda):
