@@ -17,6 +17,11 @@ constexpr int kTX = 16, kTY = 16;             // columns per CTA
 constexpr int kConsumers = kTX * kTY;          // 8 consumer warps
 constexpr int kThreads = kConsumers + 32;      // + 1 producer warp
 constexpr int kNStage = kNStageDefault;        // stages in the ring (views per stage: 4, 2 or 1)
+// Resident CTAs the register budget of a back-projection kernel is sized for: three for short
+// z-runs (72 registers, no spills; the box ring decides whether a third CTA fits), two for
+// ZU = 64 (64 accumulators).
+template <int ZU, int VPS>
+constexpr int kFdkMinCtas = (ZU == 16 || (ZU == 32 && VPS == 1)) ? 3 : 2;
 // TMA x coordinate per box sample: pair boxes (y, dy) are two FP32 elements per sample
 template <typename TP> constexpr int kXS = sizeof(TP) == 8 ? 2 : 1;
 

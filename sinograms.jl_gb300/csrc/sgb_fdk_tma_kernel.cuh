@@ -26,11 +26,6 @@
 namespace sgb {
 namespace fdkdev {
 
-// Resident CTAs the register budget is sized for: three for short z-runs (72 registers, no
-// spills; the box ring decides whether a third CTA fits), two for ZU = 64 (64 accumulators).
-template <int ZU, int VPS>
-constexpr int kFdkMinCtas = (ZU == 16 || (ZU == 32 && VPS == 1)) ? 3 : 2;
-
 template <typename TP, bool ARC, int ZU, int BW, int VPS, int NSTAGE>
 __global__ void __launch_bounds__(kThreads, (kFdkMinCtas<ZU, VPS>))
     fdk_tma_kernel(FdkTmaArgs A, const __grid_constant__ CUtensorMap map) {
