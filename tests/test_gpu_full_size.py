@@ -1,10 +1,10 @@
-"""Parity at the full BASELINE sizes.
+"""Parity at the full benchmark sizes.
 
-* config 3 (CtFanFlat 512x384x720 -> 512x512x256, the benchmark): every 16th voxel in x and
+* CBCT flat panel (CtFanFlat 512x384x720 -> 512x512x256, the benchmark): every 16th voxel in x and
   y on every 32nd slice against the FP64 oracle (the oracle filters every detector row by
   FFT and back-projects the sampled voxels); exact scaling fdk(2p) == 2 fdk(p) and
   additivity on the whole volume;
-* config 1 (SinoPar 256 x 180, Hann) and config 2 (SinoFanArc 888 x 512 views over a short
+* 2D parallel beam (SinoPar 256 x 180, Hann) and 2D fan arc (SinoFanArc 888 x 512 views over a short
   scan, Parker, noisy): whole images against the FP64 oracle, compared inside the
   reconstruction FOV."""
 import math
@@ -26,7 +26,7 @@ def _workers():
 
 
 @pytest.fixture(scope="module")
-def config3(cuda):
+def cbct_flat_512(cuda):
     import torch
     rg = S.CtFanFlat(**GEOM3)
     ig = S.ImageGeom((512, 512, 256), (0.5, 0.5, 0.5))
@@ -38,8 +38,8 @@ def config3(cuda):
     return rg, ig, plan, proj, img
 
 
-def test_config3_sampled_voxels_match_fp64_oracle(config3):
-    rg, ig, plan, proj, img = config3
+def test_cbct_flat_512_sampled_voxels_match_fp64_oracle(cbct_flat_512):
+    rg, ig, plan, proj, img = cbct_flat_512
     g = dict(kind="flat", offset_s=0.0, offset_t=0.0, orbit_start=0.0, source_offset=0.0, **GEOM3)
     p = proj.cpu().numpy().astype(np.float64)
     filt = O.sino_filter_fft(p * O.fdk_weights(g), O.fbp_filter(g), workers=_workers())
@@ -53,9 +53,9 @@ def test_config3_sampled_voxels_match_fp64_oracle(config3):
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
-def test_config3_scaling_is_exact_and_sums_add(config3):
+def test_cbct_flat_512_scaling_is_exact_and_sums_add(cbct_flat_512):
     import torch
-    rg, ig, plan, proj, img = config3
+    rg, ig, plan, proj, img = cbct_flat_512
     twice = S.fdk(plan, 2 * proj)
     assert torch.equal(twice, 2 * img)  # every rounding commutes with scaling by 2
     other = S.ellipsoid_proj(rg, S.random_ellipsoids(12, 33, 100.0, 50.0), device=True)
@@ -65,7 +65,7 @@ def test_config3_scaling_is_exact_and_sums_add(config3):
     assert rel < 1e-6
 
 
-def test_config1_full_size_par_hann(cuda):
+def test_par_256x180_hann_full_size(cuda):
     g = dict(kind="par", nb=256, d=1.0, offset=0.0, na=180, orbit=180.0, orbit_start=0.0)
     igd = dict(dims=(256, 256), deltas=(1.0, 1.0))
     ell = S.random_ellipses(10, 1, 100.0)
@@ -81,7 +81,7 @@ def test_config1_full_size_par_hann(cuda):
     assert np.abs(out - ref)[inside].max() <= 1e-4 * np.abs(ref).max()
 
 
-def test_config2_full_size_arc_short_scan_noisy(cuda):
+def test_fan_arc_888x512_short_scan_noisy_full_size(cuda):
     base = dict(kind="arc", nb=888, d=1.0239, offset=0.0, dsd=949.075, dod=408.075, source_offset=0.0,
                 orbit_start=0.0)
     orbit = 180 + 2 * math.degrees(float(np.max(np.abs(O.gamma(dict(base, na=2, orbit=360.0))))))

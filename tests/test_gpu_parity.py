@@ -4,7 +4,7 @@ the GPU path.
 
 Tolerances (FP32 arithmetic against FP64): relative RMSE <= 1e-5 and max abs error
 <= 1e-4 * max|ref| for the FP32 forms; <= 1e-4 relative RMSE for the BF16 storage form
-(the benchmark spec's bound)."""
+(the accuracy bound stated for that form)."""
 import math
 import os
 
