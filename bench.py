@@ -696,6 +696,34 @@ def run_dd_case(args):
                       "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
 
 
+def run_fbp2d_case(args):
+    """The three 2D workloads for a back-projector capture: SinoPar 256 x 180 -> 256^2 (Hann),
+    SinoFanFlat 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
+    over a short scan -> 512^2, each planned once, then three rounds of one fbp(plan, sino) per
+    workload in that order (three back2_kernel launches per round)."""
+    import torch
+
+    import sinograms as S
+    from sinograms import learned as LF
+    cases = []
+    rg = S.SinoPar(nb=256, d=1.0, na=180, orbit=180.0)
+    cases.append((S.plan_fbp(rg, S.ImageGeom((256, 256), (1.0, 1.0)), window=S.Window("hann")),
+                  S.ellipse_sino(rg, S.random_ellipses(10, 1, 100.0), device=True)))
+    rg, ig = LF.sparse_fan_geometry()
+    cases.append((S.plan_fbp(rg, ig), S.ellipse_sino(rg, LF.phantom_ellipses(900000), device=True)))
+    base = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=2, orbit=360.0)
+    orbit = 180.0 + 2.0 * float(np.degrees(S._gamma_max(base)))
+    rg = S.SinoFanArc(nb=888, d=1.0239, dsd=949.075, dod=408.075, na=512, orbit=orbit)
+    cases.append((S.plan_fbp(rg, S.ImageGeom((512, 512), (0.9766, 0.9766))),
+                  S.ellipse_sino(rg, S.random_ellipses(20, 2, 220.0, axes=(4.0, 120.0), dens=(-0.3, 1.0)),
+                                 device=True)))
+    sums = []
+    for _ in range(3):
+        sums = [float(S.fbp(plan, sino).sum()) for plan, sino in cases]
+    torch.cuda.synchronize()
+    print(json.dumps({"case": "fbp2d_par256x180_flat888x90_arc888x512", "image_sums": sums}))
+
+
 def run_case(args):
     """Reduced profiling case (one GPU, a few launches): fdk of 512x512x64 voxels from
     180 views of the benchmark geometry; the filtered projections (141 MB) exceed L2."""
@@ -706,6 +734,8 @@ def run_case(args):
         return run_batch_case(args)
     if args.case == "dd-fanflat-888x90":
         return run_dd_case(args)
+    if args.case == "fbp-2d":
+        return run_fbp2d_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -728,7 +758,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fanflat-888x90"],
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fanflat-888x90", "fbp-2d"],
                     help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
     args = ap.parse_args()
