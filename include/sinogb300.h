@@ -301,6 +301,12 @@ SGB_API int sgb_lf_loss_grad(sgb_lf *lf, const float *z, const float *target, lo
 /* one Adam step (lr; beta 0.9/0.999) on the batch; *loss (optional) is the pre-step loss */
 SGB_API int sgb_lf_train_step(sgb_lf *lf, const float *z, const float *target, long long rows, int L,
                               float lr, double *loss, int flags, void *stream);
+/* Checkpoint and resume of training (no counterpart in the reference): the Adam moments m and
+ * v (nparam FP32 values each, in the layout of the params) and the number of steps taken.
+ * Together with sgb_lf_get_params / sgb_lf_create(params) they restore a filter whose next
+ * train steps equal those of the filter that was saved.  Both wait for the device first. */
+SGB_API int sgb_lf_get_state(const sgb_lf *lf, float *m, float *v, long long *step);
+SGB_API int sgb_lf_set_state(sgb_lf *lf, const float *m, const float *v, long long step);
 SGB_API int sgb_lf_destroy(sgb_lf *lf);
 
 /* ------------------------------------------------------ failure detection */

@@ -805,6 +805,26 @@ int sgb_lf_train_step(sgb_lf *F, const float *z, const float *target, long long 
     return SGB_OK;
 }
 
+// Adam state for checkpoint and resume.  Both calls first wait for all work on the device, so
+// a train step enqueued asynchronously on any stream has finished before the state moves.
+int sgb_lf_get_state(const sgb_lf *F, float *m, float *v, long long *step) {
+    SGB_REQUIRE(F && m && v && step, "lf_get_state: bad argument");
+    SGB_CUDA(cudaDeviceSynchronize());
+    SGB_CUDA(cudaMemcpy(m, F->m.p, sizeof(float) * F->nparam, cudaMemcpyDeviceToHost));
+    SGB_CUDA(cudaMemcpy(v, F->v.p, sizeof(float) * F->nparam, cudaMemcpyDeviceToHost));
+    *step = F->step;
+    return SGB_OK;
+}
+
+int sgb_lf_set_state(sgb_lf *F, const float *m, const float *v, long long step) {
+    SGB_REQUIRE(F && m && v && step >= 0, "lf_set_state: bad argument");
+    SGB_CUDA(cudaDeviceSynchronize());
+    SGB_CUDA(cudaMemcpy(F->m.p, m, sizeof(float) * F->nparam, cudaMemcpyHostToDevice));
+    SGB_CUDA(cudaMemcpy(F->v.p, v, sizeof(float) * F->nparam, cudaMemcpyHostToDevice));
+    F->step = step;
+    return SGB_OK;
+}
+
 int sgb_lf_destroy(sgb_lf *F) {
     delete F;
     return SGB_OK;

@@ -104,6 +104,8 @@ _SIGS = {
     "sgb_lf_apply": (c_int, [P, P, c_ll, c_int, P, c_int, P]),
     "sgb_lf_loss_grad": (c_int, [P, P, P, c_ll, c_int, P, P, c_int, P]),
     "sgb_lf_train_step": (c_int, [P, P, P, c_ll, c_int, c_float, P, c_int, P]),
+    "sgb_lf_get_state": (c_int, [P, P, P, P]),
+    "sgb_lf_set_state": (c_int, [P, P, P, c_ll]),
     "sgb_lf_destroy": (c_int, [P]),
     "sgb_batch_fdk_create": (c_int, [c_int, P, P, P, P]),
     "sgb_batch_fdk_set_input": (c_int, [P, c_int, P, c_int, P]),

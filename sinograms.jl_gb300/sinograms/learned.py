@@ -84,6 +84,34 @@ class LearnedFilter:
         d = np.load(path)
         return cls(float(d["scale"]), d["params"])
 
+    def adam_state(self):
+        """(m, v, step): the Adam moments (FP32, the params' layout) and the steps taken."""
+        m = np.zeros(self.nparam, dtype=np.float32)
+        v = np.zeros(self.nparam, dtype=np.float32)
+        step = ctypes.c_longlong()
+        _status(_lib.lib().sgb_lf_get_state(self._h, ptr(m), ptr(v), ctypes.byref(step)), "lf_get_state")
+        return m, v, int(step.value)
+
+    def set_adam_state(self, m, v, step: int):
+        m = np.ascontiguousarray(m, dtype=np.float32)
+        v = np.ascontiguousarray(v, dtype=np.float32)
+        if m.size != self.nparam or v.size != self.nparam:
+            raise ValueError(f"Adam state of {m.size}/{v.size} values for a filter of {self.nparam} params")
+        _status(_lib.lib().sgb_lf_set_state(self._h, ptr(m), ptr(v), int(step)), "lf_set_state")
+
+    def save_checkpoint(self, path: str):
+        """Params, scale and Adam state: load_checkpoint(path) resumes training where it stopped."""
+        m, v, step = self.adam_state()
+        np.savez(path, params=self.params(), scale=np.float32(self.scale), adam_m=m, adam_v=v,
+                 adam_step=np.int64(step))
+
+    @classmethod
+    def load_checkpoint(cls, path: str):
+        d = np.load(path)
+        lf = cls(float(d["scale"]), d["params"])
+        lf.set_adam_state(d["adam_m"], d["adam_v"], int(d["adam_step"]))
+        return lf
+
     def apply(self, z, sync: bool = True):
         """y = z + scale * net(z / scale) for rows z of shape (..., L); with CUDA tensors and
         sync=False the call only enqueues work on the current stream."""
