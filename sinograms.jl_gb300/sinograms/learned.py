@@ -249,16 +249,26 @@ def make_dataset(n_phantoms: int, seed: int, rg=None, ig=None, noise: float = 0.
 
 
 def train(lf: LearnedFilter, zn, zc, epochs: int = 2, batch: int = 4096, lr: float = 1e-3, seed: int = 0,
-          log=None):
-    """Adam over shuffled row batches; returns the per-step losses."""
-    g = torch.Generator(device="cuda").manual_seed(seed)
+          log=None, start: int = 0, stop: int | None = None):
+    """Adam over shuffled row batches with a cosine-decayed rate; returns the per-step losses.
+    Runs steps start .. stop-1 of the epochs * (rows // batch) step schedule, so a filter saved by
+    save_checkpoint after k steps and restored by load_checkpoint continues with start = k (the
+    shuffles of the epochs already done are drawn again from the seeded generator, on the
+    rows' device)."""
+    dev = zn.device
+    g = torch.Generator(device=dev).manual_seed(seed)
     R = zn.shape[0]
+    per = R // batch
     losses = []
-    steps = epochs * (R // batch)
-    for step in range(steps):
-        if step % (R // batch) == 0:
-            perm = torch.randperm(R, device="cuda", generator=g)
-        j = step % (R // batch)
+    steps = epochs * per
+    stop = steps if stop is None else min(stop, steps)
+    for _ in range(start // per):
+        torch.randperm(R, device=dev, generator=g)
+    perm = None
+    for step in range(start, stop):
+        j = step % per
+        if j == 0 or perm is None:
+            perm = torch.randperm(R, device=dev, generator=g)
         idx = perm[j * batch:(j + 1) * batch]
         rate = lr * 0.5 * (1 + math.cos(math.pi * step / steps))  # cosine decay
         losses.append(lf.train_step(zn[idx].contiguous(), zc[idx].contiguous(), max(rate, 1e-6)))

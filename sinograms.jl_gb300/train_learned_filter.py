@@ -4,6 +4,9 @@ kernels) and evaluate it against plain ramp FBP on held-out scans.
     python sinograms.jl_gb300/train_learned_filter.py [--phantoms 20000] [--out PATH]
     python sinograms.jl_gb300/train_learned_filter.py --linear [--phantoms 2000] [--out PATH]
 
+Checkpoint and resume: `--stop K --checkpoint PATH` ends after K steps of the schedule and saves
+params, scale and Adam state; `--resume PATH` (with the same data arguments) continues from there.
+
 --linear fits the learned linear filter instead (LearnedRamp: the ramp response times the
 least-squares per-frequency gain) and compares it with plain FBP at the same latency.
 
@@ -109,6 +112,9 @@ def main():
     ap.add_argument("--out", default=LF.default_weights_path())
     ap.add_argument("--eval-only", action="store_true", help="evaluate the weights at --out without training")
     ap.add_argument("--linear", action="store_true", help="fit the learned linear (ramp) filter instead")
+    ap.add_argument("--checkpoint", help="save params, scale and Adam state here when the run stops")
+    ap.add_argument("--stop", type=int, help="stop after this many steps of the schedule (with --checkpoint)")
+    ap.add_argument("--resume", help="continue the schedule from a checkpoint (same data arguments)")
     args = ap.parse_args()
     rg, ig = LF.sparse_fan_geometry()
     if args.linear:
@@ -133,17 +139,31 @@ def main():
     torch.cuda.synchronize()
     t_data = time.perf_counter() - t0
     scale = float(zc.pow(2).mean().sqrt())
-    lf = LF.LearnedFilter(scale=scale, seed=args.seed)
+    if args.resume:
+        lf = LF.LearnedFilter.load_checkpoint(args.resume)
+        start = lf.adam_state()[2]
+    else:
+        lf = LF.LearnedFilter(scale=scale, seed=args.seed)
+        start = 0
+    steps = args.epochs * (zn.shape[0] // args.batch)
     t0 = time.perf_counter()
-    losses = LF.train(lf, zn, zc, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed)
+    losses = LF.train(lf, zn, zc, epochs=args.epochs, batch=args.batch, lr=args.lr, seed=args.seed, start=start,
+                      stop=args.stop)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del zn, zc
+    if args.checkpoint:
+        lf.save_checkpoint(args.checkpoint)
+    done = lf.adam_state()[2]
+    if done < steps:  # a partial run leaves the weights file alone
+        print(json.dumps({"steps_done": done, "steps_total": steps, "checkpoint": args.checkpoint,
+                          "loss_last": float(np.mean(losses[-20:])) if losses else None}))
+        return
     os.makedirs(os.path.dirname(args.out), exist_ok=True)
     lf.save(args.out)
     print(json.dumps({
         "phantoms": args.phantoms, "rows": args.phantoms * rg.na, "epochs": args.epochs, "batch": args.batch,
-        "steps": len(losses), "data_seconds": t_data, "train_seconds": t_train, "scale": scale,
+        "steps": len(losses), "data_seconds": t_data, "train_seconds": t_train, "scale": lf.scale,
         "loss_first": losses[0], "loss_last": float(np.mean(losses[-20:])), "weights": args.out,
         **summary(lf, plan, rg, ig, args.eval)}))
 

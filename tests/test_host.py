@@ -191,3 +191,29 @@ def test_learned_ramp_gain_file_and_round_trip(tmp_path):
     assert np.array_equal(back.gain, g) and back.npad == lr.npad and back.meta["phantoms"] == lr.meta["phantoms"]
     with pytest.raises(S.SinogramsArgumentError):
         LF.LearnedRamp(g[:-1], lr.npad)
+
+
+def test_learned_training_schedule_resumes_where_it_stopped():
+    """train(start=k) after train(stop=k) takes the same batches at the same rates as one
+    uninterrupted run (the seeded shuffles of finished epochs are drawn again), so a filter
+    restored from a checkpoint continues the schedule it was saved in."""
+    import torch
+    from sinograms import learned as LF
+
+    class Recorder:  # stands in for the GPU filter: records each step's rows and rate
+        def __init__(self):
+            self.steps = []
+
+        def train_step(self, z, t, rate):
+            self.steps.append((z[:, 0].tolist(), rate))
+            return 0.0
+
+    zn = torch.arange(1000, dtype=torch.float32)[:, None].repeat(1, 3)
+    full = Recorder()
+    LF.train(full, zn, zn, epochs=3, batch=64, seed=7)
+    assert len(full.steps) == 3 * (1000 // 64)
+    for k in (1, 15, 16, 31, 44):
+        a, b = Recorder(), Recorder()
+        LF.train(a, zn, zn, epochs=3, batch=64, seed=7, stop=k)
+        LF.train(b, zn, zn, epochs=3, batch=64, seed=7, start=k)
+        assert a.steps + b.steps == full.steps, k
