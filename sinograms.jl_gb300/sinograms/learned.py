@@ -51,12 +51,19 @@ def sparse_fan_geometry(na: int = 90):
     return rg, ig.with_mask(ig.circle(_rfov(rg)))
 
 
+# the network's shape: 1 -> 32 -> 32 -> 32 -> 32 -> 1 channels, kernel 9 (W then b per layer)
+_CHANNELS = (1, 32, 32, 32, 32, 1)
+NPARAM = sum(ci * co * 9 + co for ci, co in zip(_CHANNELS[:-1], _CHANNELS[1:]))
+
+
 class LearnedFilter:
     """Handle of a learned row filter (sgb_lf)."""
 
     def __init__(self, scale: float = 1.0, params=None, seed: int = 0):
         self._h = ctypes.c_void_p()
-        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32)
+        p = None if params is None else np.ascontiguousarray(params, dtype=np.float32).ravel()
+        if p is not None and p.size != NPARAM:
+            raise ValueError(f"learned filter: {p.size} params given, the network has {NPARAM}")
         _status(_lib.lib().sgb_lf_create(ctypes.c_float(scale), ptr(p), ctypes.c_ulonglong(seed),
                                          ctypes.byref(self._h)), "lf_create")
         self.scale = float(scale)

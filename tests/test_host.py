@@ -217,3 +217,13 @@ def test_learned_training_schedule_resumes_where_it_stopped():
         LF.train(a, zn, zn, epochs=3, batch=64, seed=7, stop=k)
         LF.train(b, zn, zn, epochs=3, batch=64, seed=7, start=k)
         assert a.steps + b.steps == full.steps, k
+
+
+def test_learned_filter_refuses_params_of_the_wrong_size():
+    """sgb_lf_create reads nparam floats from its pointer, so the host side checks the count
+    (the network's shape gives it; the FP64 oracle of the network agrees) before the call."""
+    import learned_oracle as LO
+    from sinograms import learned as LF
+    assert LF.NPARAM == LO.nparams() == 28353
+    with pytest.raises(ValueError):
+        LF.LearnedFilter(scale=1.0, params=np.zeros(LF.NPARAM - 1, np.float32))
