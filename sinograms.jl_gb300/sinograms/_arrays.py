@@ -67,6 +67,33 @@ def empty(shape, like: Arr, dtype=np.float32):
     return np.empty(shape, dtype=dtype)
 
 
+def check_out(out, shape, device: bool):
+    """Raise ValueError unless `out` can take the library's prod(shape) float32 writes: a
+    C-contiguous float32 array of exactly `shape`, a CUDA tensor when `device` (the input is on
+    the GPU), else a numpy array or CPU tensor."""
+    shape = tuple(shape)
+    if torch is not None and isinstance(out, torch.Tensor):
+        ok = (out.is_cuda == device and out.dtype == torch.float32 and out.is_contiguous()
+              and tuple(out.shape) == shape)
+    else:
+        ok = (not device and isinstance(out, np.ndarray) and out.dtype == np.float32
+              and out.flags.c_contiguous and out.flags.writeable and out.shape == shape)
+    if not ok:
+        where = "a CUDA tensor" if device else "a host array"
+        desc = f"{type(out).__name__} {getattr(out, 'dtype', '')} {tuple(getattr(out, 'shape', ()))}"
+        raise ValueError(f"out must be {where}, float32, contiguous, of shape {shape}; got {desc}")
+    return out
+
+
+def out_buffer(out, shape, like: Arr):
+    """The caller's `out` (checked by check_out) or a new array in the same place as the input."""
+    if out is None:
+        return empty(shape, like)
+    if like.device and is_cuda(out) and out.device != like.obj.device:
+        raise ValueError(f"out is on {out.device}, the input on {like.obj.device}")
+    return check_out(out, shape, like.device)
+
+
 def ptr(a):
     if a is None:
         return None

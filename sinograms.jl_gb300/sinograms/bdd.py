@@ -13,7 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from ._arrays import Arr, empty, f64, flags_for, plan_call, ptr, stream_for
+from ._arrays import Arr, empty, f64, flags_for, out_buffer, plan_call, ptr, stream_for
 from .filters import SinogramsArgumentError
 from .geom import _ar, _dso
 
@@ -93,7 +93,7 @@ class BddPlan:
 
     def _call(self, fn, x, out_shape, out, sync):
         a = Arr(x)
-        y = empty(out_shape, a) if out is None else out
+        y = out_buffer(out, out_shape, a)
         flags, st = plan_call(a.device, sync)
         _lib.check(getattr(_lib.lib(), fn)(self._h, a.ptr, ptr(y), flags, st), fn)
         return y

@@ -10,7 +10,7 @@ import ctypes
 import numpy as np
 
 from . import _lib
-from ._arrays import Arr, empty, f64, flags_for, plan_call, ptr, stream_for, torch
+from ._arrays import Arr, check_out, empty, f64, flags_for, is_cuda, out_buffer, plan_call, ptr, stream_for, torch
 from .filters import SinogramsArgumentError, Window, fbp_view_weight, fdk_view_weight
 from .geom import CtFan, ImageGeom, SinoPar, _ar, _dso, _rfov, c_struct, dims, is_ct
 
@@ -136,7 +136,7 @@ def fdk(plan: FDKplan, proj, out=None, sync: bool = True):
     a = Arr(proj)
     if tuple(reversed(a.shape)) != dims(rg):
         raise SinogramsArgumentError(f"size mismatch {tuple(reversed(a.shape))} {dims(rg)}")  # fdk.jl:68-69
-    img = out if out is not None else empty(tuple(reversed(plan.ig.dims)), a)
+    img = out_buffer(out, tuple(reversed(plan.ig.dims)), a)
     flags, st = plan_call(a.device, sync)
     _status(_lib.lib().sgb_fdk(plan.handle, a.ptr, ptr(img), flags, st), "fdk")
     return img
@@ -150,7 +150,7 @@ def _fbp_plan(plan: FBPNormalPlan, sino, out=None, sync=True):
         raise SinogramsArgumentError("bad sino size")  # fbp.jl:80
     nsl = int(np.prod(shp[2:])) if len(shp) > 2 else 1
     oshape = tuple(reversed(plan.ig.dims)) if len(shp) == 2 else tuple(a.shape[:-2]) + tuple(reversed(plan.ig.dims))
-    img = out if out is not None else empty(oshape, a)
+    img = out_buffer(out, oshape, a)
     flags, st = plan_call(a.device, sync)
     _status(_lib.lib().sgb_fbp(plan.handle, a.ptr, ptr(img), nsl, flags, st), "fbp")
     return img
@@ -279,7 +279,8 @@ class FDKBatch:
                 out = torch.empty(shape, dtype=torch.float32, device="cuda")
             else:
                 out = np.empty(shape, dtype=np.float32)
-        dev = not isinstance(out, np.ndarray)
+        dev = is_cuda(out)
+        check_out(out, shape, dev)
         _status(_lib.lib().sgb_batch_fdk_get_output(self._h, i, ptr(out), flags_for(dev), stream_for(dev)),
                 "batch_fdk_get_output")
         return out

@@ -227,3 +227,22 @@ def test_learned_filter_refuses_params_of_the_wrong_size():
     assert LF.NPARAM == LO.nparams() == 28353
     with pytest.raises(ValueError):
         LF.LearnedFilter(scale=1.0, params=np.zeros(LF.NPARAM - 1, np.float32))
+
+
+def test_output_buffers_are_checked_before_the_library_writes():
+    """A caller's `out` must hold exactly the prod(shape) float32 values the library writes, on
+    the input's side; anything else raises instead of letting the call write out of bounds."""
+    import torch
+    from sinograms._arrays import Arr, check_out, out_buffer
+    host = Arr(np.zeros((4, 6), np.float32))
+    good = np.empty((3, 5), np.float32)
+    assert out_buffer(good, (3, 5), host) is good
+    assert out_buffer(None, (3, 5), host).shape == (3, 5)
+    t = torch.empty((3, 5))
+    assert check_out(t, (3, 5), device=False) is t
+    for bad in (np.empty((3, 4), np.float32), np.empty((3, 5), np.float64), np.empty((5, 3), np.float32).T,
+                torch.empty((3, 5), dtype=torch.float64), [0.0] * 15):
+        with pytest.raises(ValueError):
+            out_buffer(bad, (3, 5), host)
+    with pytest.raises(ValueError):  # a host array cannot take a device call's output
+        check_out(good, (3, 5), device=True)
