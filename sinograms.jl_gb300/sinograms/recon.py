@@ -183,7 +183,11 @@ def cbct_back(proj, rg, ig: ImageGeom, ia_skip: int = 1, sync: bool = True):
     """cbct_back(proj, rg, ig; ia_skip), cbct-back.jl:25-45 (pure back-projection)."""
     if not isinstance(rg, CtFan):
         raise SinogramsArgumentError("cbct_back needs a CtFan geometry")
+    if len(ig.dims) != 3:
+        raise SinogramsArgumentError("cbct_back needs a 3D ImageGeom")
     a = Arr(proj)
+    if tuple(reversed(a.shape)) != dims(rg):  # the view angles come from rg, one per projection
+        raise SinogramsArgumentError(f"proj size {tuple(reversed(a.shape))} != dims(rg) {dims(rg)}")
     na, nt, ns = a.shape
     xc, yc, zc = (f64(v) for v in ig.axes())
     betas = f64(_ar(rg))

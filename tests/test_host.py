@@ -246,3 +246,14 @@ def test_output_buffers_are_checked_before_the_library_writes():
             out_buffer(bad, (3, 5), host)
     with pytest.raises(ValueError):  # a host array cannot take a device call's output
         check_out(good, (3, 5), device=True)
+
+
+def test_cbct_back_refuses_projections_that_do_not_match_the_geometry():
+    """cbct_back takes one view angle per projection from rg, so a proj whose size differs from
+    dims(rg) is refused before the library is called (cbct-back.jl:116 checks the image sizes)."""
+    rg = S.CtFanFlat(ns=40, nt=30, na=25, ds=1.0, dt=1.0, dsd=500.0, dod=200.0)
+    ig = S.ImageGeom((20, 18, 14), (1.0, 1.0, 1.0))
+    with pytest.raises(S.SinogramsArgumentError):
+        S.cbct_back(np.zeros((26, 30, 40), np.float32), rg, ig)
+    with pytest.raises(S.SinogramsArgumentError):
+        S.cbct_back(np.zeros((25, 30, 40), np.float32), rg, S.ImageGeom((20, 18), (1.0, 1.0)))
