@@ -257,3 +257,21 @@ def test_cbct_back_refuses_projections_that_do_not_match_the_geometry():
         S.cbct_back(np.zeros((26, 30, 40), np.float32), rg, ig)
     with pytest.raises(S.SinogramsArgumentError):
         S.cbct_back(np.zeros((25, 30, 40), np.float32), rg, S.ImageGeom((20, 18), (1.0, 1.0)))
+
+
+@pytest.mark.parametrize("lang", ["c", "c++"])
+def test_public_header_compiles_alone(tmp_path, lang):
+    """include/sinogb300.h is plain C (no CUDA or torch types): it compiles on its own as C99
+    and as C++17, as a host program binding the library would include it."""
+    import shutil
+    import subprocess
+    cc = "gcc" if lang == "c" else "g++"
+    if shutil.which(cc) is None:
+        pytest.skip(f"{cc} not found")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "sinogb300.h"\nint main(void) { return sgb_version() > 0 ? 0 : 1; }\n')
+    std = "-std=c99" if lang == "c" else "-std=c++17"
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([cc, std, "-x", lang, "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
+                        "-I", os.path.join(root, "include"), str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
