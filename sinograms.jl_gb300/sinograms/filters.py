@@ -4,6 +4,7 @@ its GPU row filter."""
 from __future__ import annotations
 
 import ctypes
+import math
 from dataclasses import dataclass
 
 import numpy as np
@@ -40,8 +41,13 @@ def ramp_arc(N: int, ds: float, dsd: float):
     return h, np.arange(-(N // 2), N // 2)
 
 
-def fbp_ramp(rg, N: int):
-    """fbp_ramp(rg, N), ramp.jl:171-182."""
+def fbp_ramp(rg, N: int, dr: float | None = None):
+    """fbp_ramp(rg, N), ramp.jl:24-35; for SinoMoj the keyword ``dr`` (default rg.d) is the ray
+    spacing, which varies with the projection angle (ramp.jl:27-30)."""
+    if rg.kind == "moj":
+        return ramp_flat(N, rg.d if dr is None else dr)
+    if dr is not None:
+        raise SinogramsArgumentError("dr applies to SinoMoj only")
     if rg.kind == "arc":
         return ramp_arc(N, _ds(rg), rg.dsd)
     return ramp_flat(N, _ds(rg))
@@ -122,7 +128,12 @@ def _angle_weights(ar) -> float:
 
 def parker_weight(rg) -> np.ndarray:
     """parker_weight(rg), parker.jl:58, 111-119, 147-154, returned in numpy order:
-    SinoPar (1,1) or (na,1); SinoFan (1,1) or (na,nb); CtFan (1,1,1) or (na,1,ns)."""
+    SinoPar (1,1) or (na,1); SinoFan (1,1) or (na,nb); CtFan (1,1,1) or (na,1,ns); SinoMoj
+    (1,1) for orbits that are whole multiples of 180 degrees, an error otherwise (parker.jl:122-129)."""
+    if rg.kind == "moj":
+        if math.trunc(rg.orbit / 180) * 180 != abs(rg.orbit):
+            raise SinogramsArgumentError(f"No Parker weighting for Mojette geometry with orbit={abs(rg.orbit)}")
+        return np.ones((1, 1), dtype=np.float32)
     c = c_struct(rg)
     if is_ct(rg):
         w = np.zeros(rg.ns * rg.na, dtype=np.float32)

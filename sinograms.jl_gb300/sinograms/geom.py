@@ -48,6 +48,27 @@ class SinoPar:
 
 
 @dataclass(frozen=True)
+class SinoMoj:
+    """2D Mojette sinogram geometry (type2.jl:112-121, constructor :215-229).  ``d`` is the
+    square pixel size; a view at angle phi samples rays d * max(|cos phi|, |sin phi|) apart
+    (_d_moj, common.jl:128).  The reference gives it a ramp (fbp_ramp with ``dr``, ramp.jl:27-30)
+    and a Parker weight (parker.jl:122-129) but no reconstruction: its Mojette plan is commented
+    out (plan2.jl:165-184), so plan_fbp refuses it here as well."""
+    nb: int = 128
+    d: float = 1.0
+    offset: float = 0.0
+    na: int | None = None
+    orbit: float = 180.0
+    orbit_start: float = 0.0
+    kind = "moj"
+
+    def __post_init__(self):
+        object.__setattr__(self, "offset", _f32(self.offset))
+        if self.na is None:
+            object.__setattr__(self, "na", _default_na(self.nb))
+
+
+@dataclass(frozen=True)
 class _SinoFan:
     nb: int = 128
     d: float = 1.0
@@ -235,6 +256,12 @@ def _t(rg) -> np.ndarray:
     return rg.dt * (np.arange(rg.nt) - ((rg.nt - 1) / 2 + rg.offset_t))
 
 
+def _d_ang(rg: SinoMoj) -> np.ndarray:
+    """Ray spacing of each Mojette view, d * max(|cos|, |sin|) of its angle (common.jl:128-129)."""
+    ar = _ar(rg)
+    return rg.d * np.maximum(np.abs(np.cos(ar)), np.abs(np.sin(ar)))
+
+
 def _ds(rg) -> float:
     return rg.ds if is_ct(rg) else rg.d
 
@@ -296,7 +323,10 @@ def _source_zs(rg) -> np.ndarray:
 
 def c_struct(rg):
     """The C ABI struct (sgb_sino_geom / sgb_ct_geom) for a geometry."""
-    kind = {"par": _lib.SGB_PAR, "arc": _lib.SGB_ARC, "flat": _lib.SGB_FLAT}[rg.kind]
+    kinds = {"par": _lib.SGB_PAR, "arc": _lib.SGB_ARC, "flat": _lib.SGB_FLAT}
+    if rg.kind not in kinds:
+        raise ValueError(f"{type(rg).__name__} has no reconstruction in the library")
+    kind = kinds[rg.kind]
     if is_ct(rg):
         helix = isinstance(rg.src, CtSourceHelix)
         return _lib.CtGeomC(kind, rg.ns, rg.nt, rg.ds, rg.dt, rg.offset_s, rg.offset_t, rg.na, rg.orbit,

@@ -119,6 +119,8 @@ def plan_fbp(rg, ig: ImageGeom, window: Window = Window(), npad: int | None = No
     back-projects a CtSourceHelix scan with t' = mag * (z - source_zs[view]) -- the shift
     the reference leaves commented at cbct-back.jl:188 -- instead of ignoring the source z
     as the reference's cbct_back does."""
+    if getattr(rg, "kind", None) == "moj":  # the reference's Mojette plan is commented out (plan2.jl:165-184)
+        raise NotImplementedError("plan_fbp: the reference has no FBP for the Mojette geometry (SinoMoj)")
     if is_ct(rg):
         return FDKplan(rg, ig, window, npad, decon1, filter, storage, source_z)
     if source_z:

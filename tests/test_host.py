@@ -275,3 +275,28 @@ def test_public_header_compiles_alone(tmp_path, lang):
     r = subprocess.run([cc, std, "-x", lang, "-Wall", "-Wextra", "-Werror", "-fsyntax-only",
                         "-I", os.path.join(root, "include"), str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_sinomoj_geometry_ramp_and_parker():
+    """SinoMoj (type2.jl:112-121): the doctest defaults (type2.jl:205-213), fbp_ramp with its
+    `dr` keyword (ramp.jl:27-30; test/fbp/ramp.jl:40-52 asks for N samples for every 2D type),
+    the Parker weight (parker.jl:122-129) and the per-view ray spacing (common.jl:128-129).
+    The reference has no FBP plan for it, and neither has this library."""
+    g = S.SinoMoj()
+    assert (g.nb, g.d, g.offset, g.na, g.orbit, g.orbit_start) == (128, 1.0, 0.0, 200, 180.0, 0.0)
+    assert S.dims(g) == (128, 200)
+    rg = S.SinoMoj(d=2.0, orbit=90.0)
+    h, n = S.fbp_ramp(rg, 8)
+    assert len(h) == 8 and len(n) == 8
+    np.testing.assert_array_equal(h, S.ramp_flat(8, 2.0)[0])
+    np.testing.assert_array_equal(S.fbp_ramp(rg, 8, dr=0.5)[0], S.ramp_flat(8, 0.5)[0])
+    with pytest.raises(S.SinogramsArgumentError):
+        S.fbp_ramp(S.SinoPar(), 8, dr=0.5)
+    np.testing.assert_array_equal(S.fbp_filter(S.SinoMoj(nb=100, d=0.7)), S.fbp_filter(S.SinoPar(nb=100, d=0.7)))
+    assert S.parker_weight(S.SinoMoj(orbit=360.0)).shape == (1, 1)
+    with pytest.raises(S.SinogramsArgumentError):
+        S.parker_weight(S.SinoMoj(orbit=270.0))
+    d = S._d_ang(S.SinoMoj(d=2.0, na=4, orbit=180.0))  # views at 0, 45, 90, 135 degrees
+    np.testing.assert_allclose(d, [2.0, 2.0 / np.sqrt(2), 2.0, 2.0 / np.sqrt(2)], rtol=1e-12)
+    with pytest.raises(NotImplementedError):
+        S.plan_fbp(g, S.ImageGeom((64, 64), (1.0, 1.0)))
