@@ -1,6 +1,7 @@
 """CPU tests of the library's host side: it loads, exports every symbol the public
 header declares, and its plan-time FP64 arithmetic and error behaviour match the oracle
 and the reference (no GPU needed: these entry points run on the host)."""
+import ctypes
 import json
 import os
 import re
@@ -300,3 +301,15 @@ def test_sinomoj_geometry_ramp_and_parker():
     np.testing.assert_allclose(d, [2.0, 2.0 / np.sqrt(2), 2.0, 2.0 / np.sqrt(2)], rtol=1e-12)
     with pytest.raises(NotImplementedError):
         S.plan_fbp(g, S.ImageGeom((64, 64), (1.0, 1.0)))
+
+
+def test_learned_state_entry_points_check_arguments_without_a_gpu():
+    """sgb_lf_get_state / sgb_lf_set_state refuse a missing handle or buffer and a negative
+    step with SGB_ERR_ARG and a message, before any device work."""
+    L = _lib.lib()
+    buf = np.zeros(4, np.float32)
+    p = buf.ctypes.data_as(ctypes.c_void_p)
+    assert L.sgb_lf_get_state(None, p, p, None) == _lib.SGB_ERR_ARG
+    assert "lf_get_state" in _lib.last_error()
+    assert L.sgb_lf_set_state(None, p, p, 3) == _lib.SGB_ERR_ARG
+    assert "lf_set_state" in _lib.last_error()
