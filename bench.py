@@ -715,8 +715,8 @@ def run_dd_case(args):
 def run_fbp2d_case(args):
     """The three 2D workloads for a back-projector capture: SinoPar 256 x 180 -> 256^2 (Hann),
     SinoFanFlat 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
-    over a short scan -> 512^2, each planned once, then three rounds of one fbp(plan, sino) per
-    workload in that order (three back2_kernel launches per round)."""
+    over a short scan -> 512^2, each planned once, then three passes of one fbp(plan, sino) per
+    workload in that order (three back2_kernel launches per pass)."""
     import torch
 
     import sinograms as S
