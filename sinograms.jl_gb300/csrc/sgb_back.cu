@@ -1,7 +1,7 @@
 // sgb_back.cu -- voxel/pixel-driven back-projectors.
 //
 // FDK: cbct_back_fan! / cbct_back_fan_voxel (src/fbp3/cbct-back.jl:95-213).
-// 2D:  fbp_back_par! / fbp_back_par_xy (src/fbp2/back-par.jl:360-469) and
+// 2D:  fbp_back_par! / fbp_back_par_xy (src/fbp2/back-par.jl:206-315) and
 //      fbp_back_fan! / fbp_back_fan_xy (src/fbp2/back-fan.jl:215-336).
 //
 // Per-view sin/cos come from FP64 angles (view_trig_kernel) and sit in shared memory.
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kBX *kBY) fdk_back_kernel(FdkArgs A) {
             const float sb = sc.x, cb = sc.y;
             const float xb = fmaf(x, cb, y * sb);                    // cbct-back.jl:174
             float mag, sp, w2;
-            if (GEO == 2) {  // parallel beam: the fan map with the source at infinity (back-par.jl:447)
+            if (GEO == 2) {  // parallel beam: the fan map with the source at infinity (back-par.jl:293)
                 mag = 1.f;
                 sp = xb;
                 w2 = 1.f;
@@ -206,7 +206,7 @@ __device__ __forceinline__ float atan_poly6(float q) {
 template <int M>
 __device__ __forceinline__ void b2_col(const Back2Args &A, float x, float sb, float cb, float *a, float *b) {
     if (M == B2_PAR) {
-        *a = fmaf(x, cb, A.wb);                       // back-par.jl:447
+        *a = fmaf(x, cb, A.wb);                       // back-par.jl:293
         *b = 0.f;
     } else {
         *a = fmaf(x, sb, A.dso_ds);                   // back-fan.jl:302
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(kB2X *kB2Y) back2_kernel(Back2Args A, int G) {
                 const float bb = b2_pix<M>(A, a, b, y[k], p.x, p.y, &w2, &fr, &in);
                 // floor(bb) from the bits of the round-down add bb + 1.5 * 2^23 (|bb| < 2^22).
                 // Every bb outside [1, nb) -- also |bb| >= 2^22, inf and NaN -- maps outside the
-                // segment, so j < jlim is the reference's tap rule (back-par.jl:461,
+                // segment, so j < jlim is the reference's tap rule (back-par.jl:307,
                 // back-fan.jl:328) for this tile.
                 const float m = __fadd_rd(bb, kMagic);
                 const uint32_t j = __float_as_uint(m) - jbias;

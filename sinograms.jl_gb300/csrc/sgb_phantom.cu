@@ -1,13 +1,13 @@
 // sgb_phantom.cu -- analytic line integrals of ellipses / ellipsoids.
 //
 // These stand in for ImagePhantoms.radon(rays(rg), ob) of the reference tests
-// (test/fbp2/fbp-fan.jl:106-109, test/fbp3/fdk.jl:23) and generate the synthetic
+// (test/fbp2/fbp-fan.jl:14-25, test/fbp3/fdk.jl:23) and generate the synthetic
 // benchmark inputs on the GPU.  Ray geometry follows rays(rg):
 //   2D: SinoPar (r, phi) = (s, beta); fan (r, phi) = (dso sin gamma, gamma + beta)
-//       (sino-geom.jl:368-401, common.jl:93-97);
+//       (sino-geom.jl:99-132, common.jl:93-97);
 //   3D: source (-dso sin b, dso cos b, 0), detector s-axis (cos b, sin b, 0), t along z,
 //       arc detector on the circle of radius dsd about the source
-//       (cb_arc_to_par.jl:23-43, cb_flat_to_par.jl:66-73).
+//       (cb_arc_to_par.jl:23-43, cb_flat_to_par.jl:23-30).
 #include "sgb_common.cuh"
 #include "sgb_kernels.cuh"
 

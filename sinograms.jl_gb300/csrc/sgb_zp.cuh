@@ -1,6 +1,6 @@
 // sgb_zp.cuh -- the Radon transform of the Zwart-Powell box spline (host and device).
 //
-// zwart_powell(r, phi), src/sys2/zwart_powell.jl:8-59: with z = (cos, sin, cos+sin,
+// zwart_powell(r, phi), src/sys2/zwart_powell.jl:9-58: with z = (cos, sin, cos+sin,
 // cos-sin) and N the number of |z_k| > 1e-7, BoxSp_k takes the central difference of
 // BoxSp_{k-1} along z_k (y +- z_k/2, divided by z_k; skipped when |z_k| <= 1e-7),
 // BoxSp0(y) = y^(N-1) for y > 0 and 0 otherwise, and the result is BoxSp4 / (N-1)!.

@@ -28,14 +28,14 @@ def _call(name, *args):
 # ------------------------------------------------------------------- ramp.jl
 
 def ramp_flat(N: int, ds: float):
-    """(h, n) = ramp_flat(N, ds), ramp.jl:233-238."""
+    """(h, n) = ramp_flat(N, ds), ramp.jl:86-91."""
     h = np.zeros(N)
     _call("sgb_fbp_ramp", _lib.SGB_FLAT, N, ds, 0.0, ptr(h))
     return h, np.arange(-(N // 2), N // 2)
 
 
 def ramp_arc(N: int, ds: float, dsd: float):
-    """(h, n) = ramp_arc(N, ds, dsd), ramp.jl:214-224."""
+    """(h, n) = ramp_arc(N, ds, dsd), ramp.jl:67-77."""
     h = np.zeros(N)
     _call("sgb_fbp_ramp", _lib.SGB_ARC, N, ds, dsd, ptr(h))
     return h, np.arange(-(N // 2), N // 2)
@@ -57,21 +57,21 @@ def fbp_ramp(rg, N: int, dr: float | None = None):
 
 @dataclass(frozen=True)
 class Window:
-    """Window(shape, cutoff), window.jl:260-269.  shape: "none", "boxcar", "hamming",
+    """Window(shape, cutoff), window.jl:22-31.  shape: "none", "boxcar", "hamming",
     "hann", or a vector (WindowVect)."""
     shape: object = "none"
     cutoff: float = 1.0
 
 
 def fbp_window(w: Window, N: int) -> np.ndarray:
-    """fbp_window(w, N), window.jl:298-312 (fftshift'ed)."""
+    """fbp_window(w, N), window.jl:60-74 (fftshift'ed)."""
     out = np.zeros(N)
     if isinstance(w.shape, str):
         _call("sgb_fbp_window", _lib.SGB_WIN[w.shape], float(w.cutoff), N, None, ptr(out))
     else:
         v = f64(w.shape)
         if len(v) != N:
-            raise SinogramsArgumentError("N mismatch")  # window.jl:310
+            raise SinogramsArgumentError("N mismatch")  # window.jl:72
         _call("sgb_fbp_window", _lib.SGB_WIN["vect"], float(w.cutoff), N, ptr(v), ptr(out))
     return out
 

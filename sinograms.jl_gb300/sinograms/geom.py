@@ -231,7 +231,7 @@ def is_ct(rg) -> bool:
 
 
 def dims(rg):
-    """dims(rg), sino-geom.jl:282 / ct-geom.jl:143 (Julia order)."""
+    """dims(rg), sino-geom.jl:13 / ct-geom.jl:14 (Julia order)."""
     return (rg.ns, rg.nt, rg.na) if is_ct(rg) else (rg.nb, rg.na)
 
 
@@ -246,7 +246,7 @@ def _ar(rg) -> np.ndarray:
 
 
 def _s(rg) -> np.ndarray:
-    """Detector s sample positions, sino-geom.jl:287-289 / ct-geom.jl:148-151."""
+    """Detector s sample positions, sino-geom.jl:18-20 / ct-geom.jl:19-23."""
     if is_ct(rg):
         return rg.ds * (np.arange(rg.ns) - ((rg.ns - 1) / 2 + rg.offset_s))
     return rg.d * (np.arange(rg.nb) - ((rg.nb - 1) / 2 + rg.offset))
@@ -291,7 +291,7 @@ def _rfov(rg) -> float:
 
 
 def downsample(rg, down: int):
-    """downsample(rg, down), sino-geom.jl:301-321 / ct-geom.jl:157-182."""
+    """downsample(rg, down), sino-geom.jl:32-53 / ct-geom.jl:28-55."""
     if down == 1:
         return rg
     if is_ct(rg):

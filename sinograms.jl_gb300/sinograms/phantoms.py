@@ -85,7 +85,7 @@ def random_ct_scans(n: int, seed: int, nell: int = 30):
         dsd = float(rng.uniform(800, 1200))
         rg = cls(ns=ns, nt=nt, ds=1.0, dt=1.0, na=na, dsd=dsd, dod=0.4 * dsd)
         rf = _rfov(rg)
-        zfov = 0.6 * nt  # dso/dsd * nt * dt (ct-geom.jl:250)
+        zfov = 0.6 * nt  # dso/dsd * nt * dt (ct-geom.jl:121)
         dx = 2 * rf / (math.sqrt(2) * nx)
         dz = 0.9 * zfov / nz
         rgs.append(rg)

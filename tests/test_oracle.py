@@ -32,7 +32,7 @@ def test_window_known_answers():
 
 def _ar32(g):
     """The reference's Float32 angles: range(orbit_start, length=na, step=orbit/na) in
-    Float32, times Float32(deg2rad(1)) (common.jl:27-34, unit.jl:161)."""
+    Float32, times Float32(deg2rad(1)) (common.jl:27-34, unit.jl:10)."""
     deg = (np.float64(g["orbit_start"]) + np.arange(g["na"]) * (np.float64(np.float32(g["orbit"])) / g["na"]))
     return (deg.astype(np.float32) * np.float32(math.pi / 180)).astype(np.float32)
 
