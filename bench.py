@@ -68,8 +68,16 @@ def replica_throughput(ws: int, units_per_rank: float, steps: int, max_ms: float
 
 
 def _phantom():
-    import sinograms as S
-    return S.random_ellipsoids(30, 3, 100.0, 50.0, axes=(3.0, 60.0), dens=(-0.3, 1.0))
+    from sinograms.phantoms import random_ellipsoids  # seeded numpy table (no library call)
+    return random_ellipsoids(30, 3, 100.0, 50.0, axes=(3.0, 60.0), dens=(-0.3, 1.0))
+
+
+def _config(ws: int) -> dict:
+    """The workload's `config` object, the same for both arms."""
+    return {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5,
+            "storage": "fp32 filtered projections, fp32 arithmetic",
+            "updates_per_step": int(np.prod(IMG["dims"])) * GEOM["na"],
+            "l2": "inputs larger than L2 (566 MB projections per step)", "parallelism": f"replicas x{ws}"}
 
 
 def _oracle_geom():
@@ -232,7 +240,7 @@ def run_ours(args):
     st = torch.cuda.current_stream()
     forms = {}
     outs = {}
-    for storage in ("f32", "bf16"):
+    for storage in ("f32", "bf16", "f16"):
         plan = S.plan_fbp(rg, ig, storage=storage)
         plan.set_timing(True)
         img = torch.empty(tuple(reversed(IMG["dims"])), dtype=torch.float32, device="cuda")
@@ -288,6 +296,13 @@ def run_ours(args):
             plans[i].sync()
     e2e_s = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
     barrier()
+    # the same public call on one plan and one stream, each step waiting for its volume: the
+    # copies do not overlap any compute
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        S.fdk(plans[0], hp, out=himgs[0])
+    e2e_1s = max_over_ranks(time.perf_counter() - t0, ws, "cuda")
+    barrier()
     e2e_ok = bool(np.allclose(himgs[(args.steps - 1) % 2], outs[head].cpu().numpy(), rtol=0, atol=1e-6 * float(
         outs[head].abs().max())))
 
@@ -304,17 +319,20 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic: 30 seeded random ellipsoids, analytic cone-beam "
         "projections generated on the GPU",
-        "config": {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5,
-                   "storage": "fp32 filtered projections, fp32 arithmetic", "updates_per_step": upd,
-                   "l2": "inputs larger than L2 (566 MB projections per step)", "parallelism": f"replicas x{ws}"},
+        "config": _config(ws),
         "forms": {k: {"value": v["value"], "ms_per_step": v["ms_per_step"], "filter_ms": v["filter_ms"],
-                      "back_ms": v["back_ms"]} for k, v in forms.items()},
+                      "back_ms": v["back_ms"], "vs_f32": v["value"] / forms["f32"]["value"],
+                      "plan": v["plan"].info()} for k, v in forms.items()},
         "e2e": {"value": replica_throughput(ws, upd, args.steps, e2e_s * 1e3), "unit": UNIT,
                 "h2d_bytes_per_step": proj.numel() * 4, "d2h_bytes_per_step": nvox * 4,
                 "ms_per_step": e2e_s * 1e3 / args.steps,
                 "pipeline": "fdk(plan, host proj) with pinned buffers; steps alternate over two plans on two "
                             "streams, so a step's copies overlap the other's compute",
-                "volume_matches_device_run": e2e_ok},
+                "volume_matches_device_run": e2e_ok,
+                "single_stream": {"value": replica_throughput(ws, upd, args.steps, e2e_1s * 1e3),
+                                  "ms_per_step": e2e_1s * 1e3 / args.steps,
+                                  "pipeline": "fdk(plan, host proj, out=host volume) on one plan and one stream, "
+                                              "synchronous: copies in, filter, back-projection, copy out"}},
         "roofline": {"bound": "hbm", "kernel": "fdk_tma_kernel", "achieved": achieved, "peak": hbm,
                      "unit": "GB/s", "frac": achieved / hbm, "peak_source": hbm_src,
                      "alg_bytes_per_launch": alg_bytes,
@@ -336,6 +354,13 @@ def run_ours(args):
             line["batched"] = measure_batched(args)
         except Exception as e:
             line["batched"] = {"error": f"{type(e).__name__}: {e}"}
+        for form in ("f16", "bf16"):
+            try:
+                b = measure_batched(args, storage=form, rerun_check=False)
+                line["batched"].setdefault("forms", {})[form] = {
+                    k: b[k] for k in ("value", "ms_per_run", "stage_ms", "box_classes", "back_updates_per_s_by_class")}
+            except Exception as e:
+                line["batched"].setdefault("forms", {})[form] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_2d:
         line["configs_2d"] = measure_2d(args)
     if ws == 1 and rank == 0 and not args.no_cpu:
@@ -343,7 +368,8 @@ def run_ours(args):
             base, acc = cpu_leg({k: v.cpu().numpy() for k, v in outs.items()}, proj.cpu().numpy())
             line["cpu_baseline"] = base
             line["accuracy_vs_fp64"] = acc
-            line["forms"]["bf16"]["meets_1e-4"] = bool(acc["bf16"]["rel_rmse"] <= 1e-4)
+            for k_ in line["forms"]:
+                line["forms"][k_]["meets_1e-4"] = bool(acc[k_]["rel_rmse"] <= 1e-4)
         except Exception as e:
             line["cpu_baseline"] = {"error": f"{type(e).__name__}: {e}"}
     if rank == 0:
@@ -352,16 +378,17 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-def measure_batched(args):
+def measure_batched(args, storage: str = "f32", rerun_check: bool = True):
     """Batched FDK workload: 48 seeded CBCT scans of uneven size (volumes 128^3 .. 384x384x256,
     na 180..720, ns 256..768, nt 128..384, flat/arc) reconstructed by one CUDA graph with one
-    persistent back-projection launch; FP32 storage.  Device-resident inputs."""
+    persistent back-projection launch per box class; `storage` form of the filtered
+    projections.  Device-resident inputs."""
     import torch
 
     import sinograms as S
     rgs, igs, ells = S.random_ct_scans(48, 4)
     t0 = time.perf_counter()
-    batch = S.FDKBatch(rgs, igs)
+    batch = S.FDKBatch(rgs, igs, storage=storage)
     t_plan = time.perf_counter() - t0
     projs = []
     for i, (rg, e) in enumerate(zip(rgs, ells)):
@@ -384,13 +411,17 @@ def measure_batched(args):
     stages = batch.timing()
     # every persistent launch does its work on every run: with all inputs doubled, every scan's
     # volume must come out exactly doubled (scaling by 2 is exact in every stage)
-    first = [batch.get_output(i, device=True) for i in range(len(rgs))]
-    for i, p in enumerate(projs):
-        batch.set_input(i, 2 * p)
-    batch.run()
-    doubled = all(bool(torch.equal(batch.get_output(i, device=True), 2 * first[i])) for i in range(len(rgs)))
-    del first, projs
-    return {"workload": "fdk_batch_48_uneven_scans_seed4", "value": info["updates"] / (ms / 1e3), "unit": UNIT,
+    doubled = None
+    if rerun_check:
+        first = [batch.get_output(i, device=True) for i in range(len(rgs))]
+        for i, p in enumerate(projs):
+            batch.set_input(i, 2 * p)
+        batch.run()
+        doubled = all(bool(torch.equal(batch.get_output(i, device=True), 2 * first[i])) for i in range(len(rgs)))
+        del first
+    del projs, batch
+    return {"workload": "fdk_batch_48_uneven_scans_seed4", "storage": storage, "value": info["updates"] / (ms / 1e3),
+            "unit": UNIT,
             "ms_per_run": ms, "updates_per_run": info["updates"], "scans": info["scans"],
             "work_items": info["work_items"], "persistent_ctas": info["ctas"], "persistent_launches": info["launches"],
             "plan_seconds": t_plan, "gpu_launches_per_run": (S.launch_count() - l0) / args.steps,
@@ -435,10 +466,10 @@ def _accuracy_2d(out, g, igd, sino, window, rfov):
 def measure_2d(args):
     """The 2D workloads beside the headline, device-resident, on seeded synthetic inputs:
     SinoPar 256 x 180 -> 256^2 with a Hann window; SinoFanArc 888 x 512 views over a short scan ->
-    512^2 (Parker weights, 0.5% noise); and the learned row filter's sparse-view scan (888 x 90
-    views over 360 deg -> 512^2, flat detector): plain FBP against FBP with the CNN row filter and
-    with the learned linear (ramp) filter, time and image RMSE against the phantom on 8 held-out
-    scans."""
+    512^2 (Parker weights, 0.5% noise); and the learned row filter's sparse-view scan (SinoFanArc
+    888 x 90 views over 360 deg -> 512^2): plain FBP against FBP with the CNN row filter and with
+    the learned linear (ramp) filter, time and image RMSE against the phantom on 8 held-out scans;
+    the data come from the arc-detector distance-driven projector."""
     import torch
 
     import sinograms as S
@@ -523,7 +554,7 @@ def measure_2d(args):
             fp32_peak = S.measure_peaks()["fp32_flops_per_s"]
         except Exception:
             fp32_peak = None
-        out["learned_filter_flat_888x90"] = {
+        out["learned_filter_arc_888x90"] = {
             "ms_plain_fbp": ms_plain, "ms_learned_fbp": ms_learned, "ms_network": ms_net,
             "network_tflops": net_flops / (ms_net / 1e3) / 1e12,
             "network_frac_of_bf16_peak": net_flops / (ms_net / 1e3) / ((_peaks().get("bf16_tflops") or FALLBACK_BF16_TFLOPS) * 1e12),
@@ -638,33 +669,36 @@ def run_reference(args):
         return
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    import sinograms as S
     rg = _oracle_geom()
     th = _threads()
-    # projections of the same phantom (GPU generator if present, else the oracle's)
-    try:
-        import torch
-        if not torch.cuda.is_available():
-            raise RuntimeError
-        proj = S.ellipsoid_proj(S.CtFanFlat(**GEOM), _phantom(), device=True).cpu().numpy()
-    except Exception:
-        proj = O.ellipsoid_proj(rg, _phantom()).astype(np.float32)
     nz = IMG["dims"][2]
     k = 8
     slabs = [np.arange(z0, z0 + k) for z0 in range(0, nz, k)]
-    for i in range(args.warmup):
-        cpu_fdk_slab(O, proj, rg, slabs[i % len(slabs)], th)
+    used = [slabs[i % len(slabs)] for i in range(args.warmup)]
+    used += [slabs[(args.warmup + i * 5) % len(slabs)] for i in range(args.steps)]
+    # projections of the same phantom by the oracle's CPU projector (this arm runs no GPU code),
+    # on the detector rows the sampled slabs reach
+    ax = O.image_axes(dict(dims=IMG["dims"], deltas=IMG["deltas"]))
+    rxy = math.hypot(abs(ax[0]).max(), abs(ax[1]).max())
+    rows = set()
+    for zi in used:
+        lo, hi = _slab_rows(rg, ax[2][zi].min(), ax[2][zi].max(), rxy)
+        rows.update(range(lo, hi + 1))
+    proj = O.ellipsoid_proj(rg, _phantom(), rows=sorted(rows)).astype(np.float32)
+    for zi in used[:args.warmup]:
+        cpu_fdk_slab(O, proj, rg, zi, th)
     tot_s, tot_u = 0.0, 0
-    for i in range(args.steps):
-        _, sec, u = cpu_fdk_slab(O, proj, rg, slabs[(args.warmup + i * 5) % len(slabs)], th)
+    for zi in used[args.warmup:]:
+        _, sec, u = cpu_fdk_slab(O, proj, rg, zi, th)
         tot_s += sec
         tot_u += u
     v = tot_u / tot_s
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "impl": "reference",
-            "data": "synthetic: 30 seeded random ellipsoids (same phantom as the GPU arm)",
-            "config": {"workload": WORKLOAD, **GEOM, "image": list(IMG["dims"]), "voxel_mm": 0.5},
+            "data": "synthetic: 30 seeded random ellipsoids (same phantom as the GPU arm), projected by the "
+                    "oracle's CPU projector on the detector rows the sampled slabs reach",
+            "config": _config(ws),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": th, "kind": "port",
                              "sample": f"each step: fdk of one {k}-slice z-slab (512x512x{k} x 720 views): weights + "
                                        "FFT ramp filter of the rows it reaches + FP32 back-projection; oracle "
@@ -689,9 +723,9 @@ def run_batch_case(args):
 
 
 def run_dd_case(args):
-    """Distance-driven projector pair on the learned-filter scan (512^2 image, 888 bins, 90 views):
-    one random-ellipse phantom projected and back-projected through its BddPlan, 5 + 20 times each,
-    device tensors, calls enqueued back to back."""
+    """Distance-driven projector pair on the learned-filter scan (512^2 image, 888 bins on the arc
+    detector, 90 views): one random-ellipse phantom projected and back-projected through its
+    BddPlan, 5 + 20 times each, device tensors, calls enqueued back to back."""
     import torch
 
     import sinograms as S
@@ -708,13 +742,13 @@ def run_dd_case(args):
         for _ in range(5):
             fn()
         ms[name] = _per_call_ms(fn, 20)
-    print(json.dumps({"case": "dd_fanflat_512x512_888x90", "ms_project": ms["project"],
+    print(json.dumps({"case": "dd_fanarc_512x512_888x90", "ms_project": ms["project"],
                       "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
 
 
 def run_fbp2d_case(args):
     """The three 2D workloads for a back-projector capture: SinoPar 256 x 180 -> 256^2 (Hann),
-    SinoFanFlat 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
+    SinoFanArc 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
     over a short scan -> 512^2, each planned once, then three passes of one fbp(plan, sino) per
     workload in that order (three back2_kernel launches per pass)."""
     import torch
@@ -737,7 +771,7 @@ def run_fbp2d_case(args):
     for _ in range(3):
         sums = [float(S.fbp(plan, sino).sum()) for plan, sino in cases]
     torch.cuda.synchronize()
-    print(json.dumps({"case": "fbp2d_par256x180_flat888x90_arc888x512", "image_sums": sums}))
+    print(json.dumps({"case": "fbp2d_par256x180_arc888x90_arc888x512", "image_sums": sums}))
 
 
 def run_case(args):
@@ -748,7 +782,7 @@ def run_case(args):
     import sinograms as S
     if args.case == "fdk-batch":
         return run_batch_case(args)
-    if args.case == "dd-fanflat-888x90":
+    if args.case == "dd-fan-888x90":
         return run_dd_case(args)
     if args.case == "fbp-2d":
         return run_fbp2d_case(args)
@@ -774,9 +808,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fanflat-888x90", "fbp-2d"],
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d"],
                     help="run a profiling case instead")
-    ap.add_argument("--storage", default="f32", choices=["f32", "bf16"], help="storage form for --case")
+    ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"], help="storage form for --case")
     args = ap.parse_args()
     if args.case:
         run_case(args)
