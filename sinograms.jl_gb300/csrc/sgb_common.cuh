@@ -19,6 +19,8 @@ void clear_error();
 const std::string &last_error();
 
 extern std::atomic<long long> g_launches;
+// device allocations made by the library (DevBuf::reserve is its only cudaMalloc)
+extern std::atomic<long long> g_device_allocs;
 
 // Status from a CUDA call; records the failing expression.
 #define SGB_CUDA(expr)                                                                        \
@@ -80,6 +82,7 @@ struct DevBuf {
             set_error("cudaMalloc(%zu) failed: %s", n, cudaGetErrorString(e));
             return SGB_ERR_NOMEM;
         }
+        g_device_allocs.fetch_add(1, std::memory_order_relaxed);
         bytes = n;
         return SGB_OK;
     }

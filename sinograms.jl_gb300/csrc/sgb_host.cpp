@@ -16,6 +16,7 @@ namespace sgb {
 
 static thread_local std::string t_err;
 std::atomic<long long> g_launches{0};
+std::atomic<long long> g_device_allocs{0};
 
 void set_error(const char *fmt, ...) {
     char buf[1024];
@@ -48,14 +49,14 @@ int next_pow2(int n) {
 }
 
 // Angles of a ray geometry in radians: range(orbit_start, length=na, step=orbit/na)
-// scaled by deg2rad(1) (common.jl:27-34, unit.jl:161).
+// scaled by deg2rad(1) (common.jl:27-34, unit.jl:10).
 std::vector<double> view_angles(int na, double orbit, double orbit_start) {
     std::vector<double> a(na);
     for (int i = 0; i < na; i++) a[i] = (orbit_start + i * (orbit / na)) * (kPi / 180.0);
     return a;
 }
 
-// _s: detector sample positions, sino-geom.jl:287-289, ct-geom.jl:148-151.
+// _s: detector sample positions, sino-geom.jl:18-20, ct-geom.jl:19-23.
 std::vector<double> det_axis(int n, double d, float offset) {
     std::vector<double> s(n);
     double w = (n - 1) / 2.0 + (double)offset;
@@ -95,10 +96,10 @@ static void real_dft(const std::vector<double> &x, std::vector<double> &out, dou
 
 int ramp_samples(int kind, int N, double ds, double dsd, std::vector<double> &h) {
     if (N % 2) {
-        set_error("N must be even");  // ramp.jl:215,234
+        set_error("N must be even");  // ramp.jl:68,87
         return SGB_ERR_ARG;
     }
-    if (kind == SGB_ARC && N / 2.0 * ds / dsd > 0.9 * kPi / 2) {  // ramp.jl:217-219
+    if (kind == SGB_ARC && N / 2.0 * ds / dsd > 0.9 * kPi / 2) {  // ramp.jl:70-72
         set_error("angle is %g degrees: too large; physically impossible arc geometry",
                   N / 2.0 * ds / dsd * 180 / kPi);
         return SGB_ERR_GEOM;
@@ -123,14 +124,14 @@ int window_samples(int shape, double cutoff, int N, const double *vect, std::vec
             set_error("WindowVect needs a vector of length N");
             return SGB_ERR_ARG;
         }
-        for (int k = 0; k < N; k++) w[k] = vect[(k + N / 2) % N];  // fftshift, window.jl:311
+        for (int k = 0; k < N; k++) w[k] = vect[(k + N / 2) % N];  // fftshift, window.jl:73
         return SGB_OK;
     }
     if (shape < SGB_WIN_NONE || shape > SGB_WIN_HANN) {
         set_error("unknown window shape %d", shape);
         return SGB_ERR_ARG;
     }
-    double width = cutoff * N;  // window.jl:299
+    double width = cutoff * N;  // window.jl:61
     for (int k = 0; k < N; k++) {
         int n = ((k + N / 2) % N) - N / 2;  // sample at fftshift'ed position k
         bool in = std::fabs((double)n) < width / 2;
@@ -138,7 +139,7 @@ int window_samples(int shape, double cutoff, int N, const double *vect, std::vec
         if (shape == SGB_WIN_BOXCAR) v = in ? 1.0 : 0.0;
         if (shape == SGB_WIN_HAMMING) v = (0.54 + 0.46 * std::cos(2 * kPi * n / width)) * in;
         if (shape == SGB_WIN_HANN) v = 0.5 * (1 + std::cos(2 * kPi * n / width)) * in;
-        w[k] = (double)(float)v;  // stored as Float32 (window.jl:298 T = Float32)
+        w[k] = (double)(float)v;  // stored as Float32 (window.jl:60 T = Float32)
     }
     return SGB_OK;
 }
@@ -224,6 +225,8 @@ int sgb_last_error(char *buf, size_t n) {
 }
 
 long long sgb_launch_count(void) { return g_launches.load(); }
+
+long long sgb_device_alloc_count(void) { return g_device_allocs.load(); }
 
 int sgb_fbp_ramp(int kind, int N, double ds, double dsd, double *h) {
     SGB_REQUIRE(h && N > 0, "fbp_ramp: bad arguments");
@@ -356,7 +359,7 @@ int sgb_footprint_size_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig, f
     }
     double smax = 0;
     for (int i = 0; i < rg->nb; i++)
-        smax = std::fmax(smax, std::fabs(rg->d * (i - ((rg->nb - 1) / 2.0 + rg->offset))));  // _s, sino-geom.jl:287
+        smax = std::fmax(smax, std::fabs(rg->d * (i - ((rg->nb - 1) / 2.0 + rg->offset))));  // _s, sino-geom.jl:20
     return footprint_fan(rg->kind, ratio, rg->dsd, rg->dsd - rg->dod, smax, ig, size);
 }
 
@@ -370,7 +373,7 @@ int sgb_footprint_size_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, float
     }
     double smax = 0;
     for (int i = 0; i < rg->ns; i++)
-        smax = std::fmax(smax, std::fabs(rg->ds * (i - ((rg->ns - 1) / 2.0 + rg->offset_s))));  // _s, ct-geom.jl:148
+        smax = std::fmax(smax, std::fabs(rg->ds * (i - ((rg->ns - 1) / 2.0 + rg->offset_s))));  // _s, ct-geom.jl:22
     return footprint_fan(rg->kind, ratio, rg->dsd, rg->dsd - rg->dod, smax, ig, size);
 }
 

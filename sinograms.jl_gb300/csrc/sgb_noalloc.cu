@@ -11,10 +11,12 @@
 // process exits.
 //
 // The first call on a device resolves the array's device address (cudaGetSymbolAddress
-// with that device current); make that first call before any stream capture.  All
-// calls on a device share the one array and it keeps the last call's contents, so
-// calls whose GPU work overlaps (different streams, or different host threads) race on
-// it: serialise them on one stream.
+// with that device current); make that first call before any stream capture begins.  The
+// address is kept for the life of the process, so the entry point must not be used on a
+// device after cudaDeviceReset (which reloads the module).  All calls on a device share
+// the one array and it keeps the last call's contents, so calls whose GPU work overlaps
+// (different streams, or different host threads) race on it: serialise them on one
+// stream.
 #include <mutex>
 
 #include "sgb_common.cuh"
@@ -81,9 +83,11 @@ extern "C" int sgb_bdd_project_noalloc(const float *phantom, int nPix, int nDet,
     void *base = nullptr;
     SGB_TRY(scratch_on_current_device(&base));
     double *angle_dev = static_cast<double *>(base);
-    // Copy of the host angle vector into the scratch; the host array may be reused as
-    // soon as the call returns.  Every other scratch byte is written by the set-up
-    // kernel before it is read, and the output is cleared by the launch itself.
+    // Copy of the host angle vector into the scratch, ordered on `stream`.  From pageable
+    // memory the copy is staged before the call returns, so the host array may be reused
+    // then; a page-locked array must stay unchanged until the stream has reached this copy.
+    // Every other scratch byte is written by the set-up kernel before it is read, and the
+    // output is cleared by the launch itself.
     SGB_CUDA(cudaMemcpyAsync(angle_dev, angle, (size_t)na * sizeof(double), cudaMemcpyHostToDevice, st));
     G.angle = angle_dev;
     return launch_bdd_project(G, phantom, sino, static_cast<char *>(base) + angle_bytes, st);

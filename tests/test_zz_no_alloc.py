@@ -6,8 +6,9 @@ memory fixed after start-up, and hosts whose device memory belongs to another al
 For them the library keeps the projector's scratch in an array of its own.  This test
 checks, on two calls in a row with different geometries (the second call reuses the
 scratch the first one left behind), that the result equals the allocating entry point
-sgb_bdd_project within the parity tolerance of the other GPU tests, and that a request
-larger than the array is refused with a clear error.  It is collected last so a failing
+sgb_bdd_project within the parity tolerance of the other GPU tests, that the calls make no
+device allocation (the library's own allocation counter, sgb_device_alloc_count, does not
+move across them), and that a request larger than the array is refused with a clear error.  It is collected last so a failing
 run that stops at the first failure has already run every other test.
 """
 import ctypes
@@ -46,7 +47,10 @@ def test_bdd_project_noalloc_matches_allocating_entry_point(cuda):
         rng = np.random.default_rng(100 + call)
         phantom = torch.as_tensor(rng.random((nPix, nPix), dtype=np.float32), device="cuda")
         out = torch.full((nDet, na), float("nan"), device="cuda")  # must be fully overwritten
+        allocs = L.sgb_device_alloc_count()
         assert _call(L.sgb_bdd_project_noalloc, phantom, out, g, angle, stream) == _lib.SGB_OK, _lib.last_error()
+        torch.cuda.synchronize()
+        assert L.sgb_device_alloc_count() == allocs, "the no-allocation entry point allocated device memory"
         ref = torch.empty((nDet, na), device="cuda")
         st = L.sgb_bdd_project(ctypes.c_void_p(phantom.data_ptr()), nPix, nDet, na,
                                ctypes.c_void_p(angle.ctypes.data), DSD, DS0, pSize, dSize,
