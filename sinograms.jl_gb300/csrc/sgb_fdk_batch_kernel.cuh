@@ -168,12 +168,14 @@ __global__ void __launch_bounds__(kThreads, (ZU == 64 ? 1 : kFdkMinCtas<ZU, VPS>
         __syncwarp();
         if (lane == 0) mbar_arrive(empty + st);
         if (tg.y == ngroups - 1 && ix < A.nx && iy < A.ny) {  // tile complete: write the voxels
+            float u = 1.f;
+            if constexpr (kQuad<TP>) u = *A.qscale;  // the scan's FP16 quad scale, undone exactly
 #pragma unroll
             for (int k = 0; k < ZU; k++) {
                 const int iz = iz0 + k;
                 if (iz >= A.nz) break;
                 const long long idx = ix + (long long)A.nx * (iy + (long long)A.ny * iz);
-                float val = acc[k];
+                float val = kQuad<TP> ? acc[k] * u : acc[k];
                 if (A.mask && !A.mask[idx]) val = 0.f;
                 A.image[idx] = val;
             }
@@ -220,7 +222,7 @@ int launch_batch_z(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, c
 
 template <typename TP>
 int launch_batch_tp(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st) {
-    if constexpr (sizeof(TP) == 8)  // ZU = 64 only for pair boxes
+    if constexpr (sizeof(TP) == 8)  // ZU = 64 only for 8-byte samples (pairs, quads)
         if (B.zu == 64) return launch_batch_z<TP, 64>(B, maps, nctas, st);
     return B.zu == 32 ? launch_batch_z<TP, 32>(B, maps, nctas, st) : launch_batch_z<TP, 16>(B, maps, nctas, st);
 }

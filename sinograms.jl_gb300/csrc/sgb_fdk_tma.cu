@@ -123,6 +123,8 @@ int fdk_tma_encode(const FdkTmaArgs &A, const void *filt, int pitch, CUtensorMap
 }
 
 int launch_fdk_tma_views(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
+    if (A.elem_bytes == 8 && A.quad)
+        return A.is_arc ? launch_fdk_tma_quad_arc(A, map, st) : launch_fdk_tma_quad_flat(A, map, st);
     if (A.elem_bytes == 8) return A.is_arc ? launch_fdk_tma_pair_arc(A, map, st) : launch_fdk_tma_pair_flat(A, map, st);
     if (A.elem_bytes == 4) return launch_fdk_tma_f32(A, map, st);
     return launch_fdk_tma_bf16(A, map, st);

@@ -17,7 +17,9 @@ struct FdkTmaArgs {
     float x0, dx, y0, dy, z0, dz;  // uniform voxel-centre axes / ds
     int is_arc;
     int zu;                 // voxels per thread along z (16 or 32)
-    int elem_bytes;         // 4 (fp32) or 2 (bf16) filtered projections
+    int elem_bytes;         // 8 (FP32 pairs or FP16 quads), 4 (FP32) or 2 (BF16) per filtered sample
+    int quad;               // 1: 8-byte samples are FP16 quads scaled by one power of two (F16 form)
+    const float *qscale;    // F16 form: device word with the factor that undoes the quads' scale
     int align;              // TMA x-coordinate alignment in elements
     int W, H, box_bytes;    // staged box (samples) and its shared-memory footprint
     int vps;                // views per pipeline stage (4, or 2 for large boxes)
@@ -48,6 +50,7 @@ struct FdkBatchArgs {
     int W;                    // common compile-time box width (32 or 64)
     int box_bytes;            // largest box of the batch
     int elem_bytes;
+    int quad;                 // 8-byte samples are FP16 quads (F16 form)
     int vps;                  // views per pipeline stage (4, 2 or 1)
     int zu;                   // voxels per thread along z of every scan in the launch (16, 32, 64)
     int nstage;               // stages of the box ring (4; 2 with one view per stage)
@@ -59,6 +62,8 @@ int launch_fdk_batch(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas,
 int launch_fdk_batch_pair(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
 int launch_fdk_batch_f32(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
 int launch_fdk_batch_bf16(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+int launch_fdk_batch_quad(const FdkBatchArgs &B, const FdkBatchMaps &maps, int nctas, cudaStream_t st);
+int fdk_batch_ctas_per_sm_quad(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm_pair(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm_f32(const FdkBatchArgs &B);
 int fdk_batch_ctas_per_sm_bf16(const FdkBatchArgs &B);
@@ -78,6 +83,8 @@ int launch_fdk_tma(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st)
 // one storage form each (sgb_fdk_tma_<form>.cu)
 int launch_fdk_tma_pair_flat(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
 int launch_fdk_tma_pair_arc(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+int launch_fdk_tma_quad_flat(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
+int launch_fdk_tma_quad_arc(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
 int launch_fdk_tma_f32(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
 int launch_fdk_tma_bf16(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st);
 

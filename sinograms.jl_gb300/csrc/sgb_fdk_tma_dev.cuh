@@ -8,6 +8,8 @@
 #include "sgb_async.cuh"
 #include "sgb_fdk_tma.cuh"
 
+#include <type_traits>
+
 namespace sgb {
 namespace fdkdev {
 
@@ -22,7 +24,17 @@ constexpr int kNStage = kNStageDefault;        // stages in the ring (views per 
 // ZU = 64 (64 accumulators).
 template <int ZU, int VPS>
 constexpr int kFdkMinCtas = (ZU == 16 || (ZU == 32 && VPS == 1)) ? 3 : 2;
-// TMA x coordinate per box sample: pair boxes (y, dy) are two FP32 elements per sample
+// FP16 quad sample of the F16 storage form (8 bytes): p = (y, y[t+1] - y) and
+// q = (y[s+1] - y, y[s+1,t+1] - y[s+1,t] - y[s,t+1] + y) as half2, every term scaled by one
+// power of two per call.  The bilinear tap of cbct-back.jl:205-208 is then
+// (y + fs dS) + ft (dT + fs dST): one 8-byte load, one half2 FMA for the s part of both rows
+// and one FMA for t.
+struct Quad16 {
+    uint32_t p, q;
+};
+template <typename TP> constexpr bool kQuad = std::is_same<TP, Quad16>::value;
+// TMA x coordinate per box sample: 8-byte samples (FP32 pairs (y, dy), FP16 quads) are two
+// FP32 elements per sample
 template <typename TP> constexpr int kXS = sizeof(TP) == 8 ? 2 : 1;
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
@@ -150,6 +162,8 @@ struct ColView {
     float fs, w2, bt0, dbt;
     int lo, hi;
     uint32_t sb;  // shared address of the box element at 1-based row 0, column of tap is-1
+    uint32_t fsh;  // FP16 quads: fs in both halves of a half2
+    unsigned short w2h;  // FP16 quads: w2 as FP16
 };
 
 template <typename TP, bool ARC, int ZU, int W>
@@ -184,14 +198,130 @@ __device__ __forceinline__ ColView view_setup(const FdkTmaArgs &A, float x, floa
         if (v0 <= v1 && (v0 < g.lo || v1 > g.hi)) atomicOr(err, 1);
     }
     g.sb = box + (uint32_t)((c - (o.y + 1) * W) * (int)sizeof(TP));  // row it (1-based) -> box row it-1-t0
-    if (r0 >= g.lo && r1 <= g.hi) g.mode = (g.dbt < 0.999f && g.dbt >= 0.f) ? 1 : 2;
-    else g.mode = 3;
+    // quads hold both rows of a tap in one sample, so they need no streaming form; their fast
+    // form rounds bt to 2^-10 (twice: the column's start, then each voxel), which may reach the
+    // row next to the first or last voxel's (one row of slack each side)
+    if constexpr (kQuad<TP>)
+        g.mode = (r0 - 1 >= g.lo && r1 + 1 <= g.hi) ? 2 : 3;
+    else if (r0 >= g.lo && r1 <= g.hi)
+        g.mode = (g.dbt < 0.999f && g.dbt >= 0.f) ? 1 : 2;
+    else
+        g.mode = 3;
+    if constexpr (kQuad<TP>) {
+        asm("cvt.rn.f16x2.f32 %0, %1, %1;" : "=r"(g.fsh) : "f"(g.fs));
+        asm("cvt.rn.f16.f32 %0, %1;" : "=h"(g.w2h) : "f"(g.w2));
+    }
     return g;
+}
+
+// Two FP32 values as a half2 (lo in the low half), round to nearest.
+__device__ __forceinline__ uint32_t pack_f16x2(float lo, float hi) {
+    uint32_t r;
+    asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+    return r;
+}
+
+__device__ __forceinline__ uint2 lds_quad(uint32_t a) {
+    uint2 v;
+    asm volatile("ld.shared.v2.b32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "r"(a));
+    return v;
+}
+
+// One FP16-quad tap: u = p + fs q (both rows' s-interpolation in one half2 FMA),
+// v = u.lo + ft u.hi, acc += w2 v with a mixed FP16 x FP16 + FP32 FMA.  `ft2` holds ft in the
+// half selected by HI.
+template <bool HI>
+__device__ __forceinline__ void quad_tap(uint2 pq, uint32_t fsh, uint32_t ft2, unsigned short w2h, float &acc) {
+    if (HI)
+        asm("{\n\t.reg .b32 u;\n\t.reg .f16 u0, u1, f, fo, v;\n\t"
+            "fma.rn.f16x2 u, %1, %3, %2;\n\t"
+            "mov.b32 {u0, u1}, u;\n\t"
+            "mov.b32 {fo, f}, %4;\n\t"
+            "fma.rn.f16 v, f, u1, u0;\n\t"
+            "fma.rn.f32.f16 %0, %5, v, %0;\n\t}"
+            : "+f"(acc)
+            : "r"(fsh), "r"(pq.x), "r"(pq.y), "r"(ft2), "h"(w2h));
+    else
+        asm("{\n\t.reg .b32 u;\n\t.reg .f16 u0, u1, f, fo, v;\n\t"
+            "fma.rn.f16x2 u, %1, %3, %2;\n\t"
+            "mov.b32 {u0, u1}, u;\n\t"
+            "mov.b32 {f, fo}, %4;\n\t"
+            "fma.rn.f16 v, f, u1, u0;\n\t"
+            "fma.rn.f32.f16 %0, %5, v, %0;\n\t}"
+            : "+f"(acc)
+            : "r"(fsh), "r"(pq.x), "r"(pq.y), "r"(ft2), "h"(w2h));
+}
+
+// Detector-row coordinate on a 2^-10 grid for the fast quad form: B = bt + 12288 lies in
+// [8192, 16384) for 1 <= bt < 4096, where the FP32 spacing is 2^-10, so an FMA that yields B
+// rounds bt to the nearest 2^-10 and leaves, in B's bits, floor(bt) + 1150976 above bit 10 and
+// the fraction's ten bits below: bits(B) = 0x46000000 + (bt + 4096) * 1024, so
+// bits(B) >> 10 = (0x46000000 >> 10) + 4096 + floor(bt) = 1150976 + floor(bt).
+constexpr float kQMagic = 12288.0f;
+constexpr uint32_t kQRowBias = (0x46000000u >> 10) + 4096u;
+static_assert(kQRowBias == 1150976u, "row bias of the 2^-10 grid");
+
+// (1 + f0, 1 + f1) as a half2 from the fraction bits of two such B values, then minus one
+// (exact): the pair's t-weights on the 2^-10 grid.
+__device__ __forceinline__ uint32_t quad_ft2(uint32_t b0, uint32_t b1) {
+    const uint32_t h = (__byte_perm(b0, b1, 0x5410) & 0x03FF03FFu) | 0x3C003C00u;
+    uint32_t r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(h), "r"(0x3C003C00u));
+    return r;
+}
+
+// FP16 quads (nt <= 4096): fast form (every voxel's rows valid and staged, with one row of
+// slack on each side) and checked form (the reference's per-voxel edge rule on FP32 bt; a
+// dropped tap reads a safe row with weight 0).  Both take the t-weight from B, bt rounded to the
+// 2^-10 grid by one FMA: the fast form reads B's row with B's fraction bits (integer units
+// only), the checked form reads the exact FP32 floor's row with weight B - 12288 - floor(bt)
+// (exact; within 2^-10 of [0, 1]).  A rounding that crosses a row boundary thus reads the
+// neighbouring row with weight 0 instead of 1 in the fast form: the same interpolated value,
+// so the two forms agree to FP16 rounding.
+template <int ZU, int W>
+__device__ __forceinline__ void view_quad(const ColView &g, float (&acc)[ZU]) {
+    constexpr uint32_t RB = W * 8;  // bytes per box row
+    static_assert(ZU % 2 == 0, "quads take voxels in pairs");
+    if (g.mode == 2) {
+        const uint32_t kb = g.sb - kQRowBias * RB;  // row bits of B -> box row address
+        const float b0 = g.bt0 + kQMagic;
+#pragma unroll
+        for (int k = 0; k < ZU; k += 2) {
+            const uint32_t m0 = __float_as_uint(fmaf((float)k, g.dbt, b0));        // :189,192
+            const uint32_t m1 = __float_as_uint(fmaf((float)(k + 1), g.dbt, b0));
+            const uint2 q0 = lds_quad(kb + (m0 >> 10) * RB), q1 = lds_quad(kb + (m1 >> 10) * RB);
+            const uint32_t ft2 = quad_ft2(m0, m1);
+            quad_tap<false>(q0, g.fsh, ft2, g.w2h, acc[k]);
+            quad_tap<true>(q1, g.fsh, ft2, g.w2h, acc[k + 1]);
+        }
+    } else if (g.mode == 3) {
+        const unsigned span = (unsigned)(g.hi - g.lo);
+        const float bm = g.bt0 + kQMagic;
+#pragma unroll
+        for (int k = 0; k < ZU; k += 2) {
+            const float b0 = fmaf((float)k, g.dbt, g.bt0), b1 = fmaf((float)(k + 1), g.dbt, g.bt0);  // :189,192
+            const float fl0 = floorf(b0), fl1 = floorf(b1);
+            const int i0 = (int)fl0, i1 = (int)fl1;
+            const bool ok0 = (unsigned)(i0 - g.lo) <= span, ok1 = (unsigned)(i1 - g.lo) <= span;  // :197
+            const uint2 q0 = lds_quad(g.sb + (uint32_t)((ok0 ? i0 : g.lo) * (int)RB));
+            const uint2 q1 = lds_quad(g.sb + (uint32_t)((ok1 ? i1 : g.lo) * (int)RB));
+            // the fast form's grid value: exact differences for valid taps (1 <= bt < 4096)
+            const float g0 = (fmaf((float)k, g.dbt, bm) - kQMagic) - fl0;
+            const float g1 = (fmaf((float)(k + 1), g.dbt, bm) - kQMagic) - fl1;
+            const uint32_t ft2 = pack_f16x2(g0, g1);
+            quad_tap<false>(q0, g.fsh, ft2, ok0 ? g.w2h : (unsigned short)0, acc[k]);
+            quad_tap<true>(q1, g.fsh, ft2, ok1 ? g.w2h : (unsigned short)0, acc[k + 1]);
+        }
+    }
 }
 
 template <typename TP, int ZU, int W>
 __device__ __forceinline__ void view_scalar(const ColView &g, float (&acc)[ZU]) {
     constexpr uint32_t RB = W * sizeof(TP);  // bytes per box row
+    if constexpr (kQuad<TP>) {
+        view_quad<ZU, W>(g, acc);
+        return;
+    }
     if (g.mode == 1) {
         // magic_floor's bits are it + 0x4B400000: fold that offset into the base address
         const uint32_t kb = g.sb - 0x4B400000u * RB;

@@ -1,6 +1,6 @@
 // sgb_fdk_tma_kernel.cuh -- the TMA-staged FDK back-projection kernel template and its
-// launchers.  Each sgb_fdk_tma_<form>.cu instantiates one storage form (FP32 pairs, FP32,
-// BF16) for the flat or arc detector, so the instantiations compile in parallel.
+// launchers.  Each sgb_fdk_tma_<form>.cu instantiates one storage form (FP32 pairs, FP16
+// quads, FP32, BF16) for the flat or arc detector, so the instantiations compile in parallel.
 //
 // Same arithmetic and edge rule as cbct_back_fan_voxel (src/fbp3/cbct-back.jl:150-213),
 // organised for sm_103a:
@@ -126,6 +126,11 @@ __global__ void __launch_bounds__(kThreads, (kFdkMinCtas<ZU, VPS>))
     }
 
     if (ix >= A.nx || iy >= A.ny) return;
+    if constexpr (kQuad<TP>) {  // undo the quads' power-of-two scale (exact)
+        const float u = *A.qscale;
+#pragma unroll
+        for (int k = 0; k < ZU; k++) acc[k] *= u;
+    }
 #pragma unroll
     for (int k = 0; k < ZU; k++) {
         const int iz = iz0 + k;
@@ -162,7 +167,7 @@ int launch_t(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
 }
 
 
-// One storage form and detector: every ZU the form offers (64 only for FP32 pairs).
+// One storage form and detector: every ZU the form offers (64 only for 8-byte samples).
 template <typename TP, bool ARC>
 int launch_form(const FdkTmaArgs &A, const CUtensorMap &map, cudaStream_t st) {
     if (A.zu == 16) return launch_t<TP, ARC, 16>(A, map, st);

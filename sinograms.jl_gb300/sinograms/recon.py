@@ -15,6 +15,9 @@ from .filters import SinogramsArgumentError, Window, fbp_view_weight, fdk_view_w
 from .geom import CtFan, ImageGeom, SinoPar, _ar, _dso, _rfov, c_struct, dims, is_ct
 
 
+_STORAGE = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16, "f16": _lib.SGB_STORE_F16}
+
+
 def _status(st: int, what: str):
     if st in (_lib.SGB_ERR_ARG, _lib.SGB_ERR_GEOM):
         raise SinogramsArgumentError(f"{what}: {_lib.last_error()}")
@@ -45,7 +48,7 @@ class _Plan:
             self._keep.append(f)
             opts.filter = f.ctypes.data
             opts.npad = len(f)
-        opts.storage = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16}[storage]
+        opts.storage = _STORAGE[storage]
         opts.source_z = int(bool(source_z))
         self._h = ctypes.c_void_p()
         g, cig = c_struct(rg), ig.c_struct()
@@ -73,10 +76,10 @@ class _Plan:
 
     def info(self) -> dict:
         """Execution layout: TMA-staged FDK kernel in use, staged box, row pitch, z-unroll."""
-        a = np.zeros(7, dtype=np.int32)
-        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 7), "plan_info")
+        a = np.zeros(8, dtype=np.int32)
+        _status(_lib.lib().sgb_plan_info(self._h, ptr(a), 8), "plan_info")
         return dict(tma=bool(a[0]), box=(int(a[1]), int(a[2])), pitch=int(a[3]), zu=int(a[4]), view_passes=int(a[5]),
-                    sample_bytes=int(a[6]))
+                    sample_bytes=int(a[6]), f16_quads=bool(a[7]))
 
     def set_view_passes(self, passes: int):
         """FDK plans: split the views over `passes` launches (overrides the autotuner's choice)."""
@@ -114,8 +117,9 @@ def plan_fbp(rg, ig: ImageGeom, window: Window = Window(), npad: int | None = No
              filter=None, storage: str = "f32", source_z: bool = False):
     """plan_fbp(rg, ig; window, npad, decon1, filter), plan2.jl:106-138 / plan3.jl:60-72.
 
-    Additions of this implementation: ``storage`` ("f32" or "bf16") selects how FDK keeps
-    the filtered projections on the GPU (2D plans always use "f32"); ``source_z=True``
+    Additions of this implementation: ``storage`` ("f32", "bf16" or "f16") selects how FDK
+    keeps the filtered projections on the GPU (2D plans always use "f32"): "f16" stores each
+    detector sample as FP16 terms of its bilinear tap, scaled by a power of two per call; ``source_z=True``
     back-projects a CtSourceHelix scan with t' = mag * (z - source_zs[view]) -- the shift
     the reference leaves commented at cbct-back.jl:188 -- instead of ignoring the source z
     as the reference's cbct_back does."""
@@ -254,7 +258,7 @@ class FDKBatch:
         opts.cutoff = float(window.cutoff)
         opts.npad = int(npad or 0)
         opts.decon1 = int(decon1)
-        opts.storage = {"f32": _lib.SGB_STORE_F32, "bf16": _lib.SGB_STORE_BF16}[storage]
+        opts.storage = _STORAGE[storage]
         opts.source_z = int(bool(source_z))
         opts.source_z = int(bool(source_z))
         self._h = ctypes.c_void_p()

@@ -85,3 +85,18 @@ def to_geom(g):
 def to_image(ig, mask=None):
     import sinograms as S
     return S.ImageGeom(ig["dims"], ig["deltas"], ig.get("offsets"), mask)
+
+
+def form_bars(storage, na):
+    """(relative RMSE, max error / max|ref|) bars of an FDK storage form on an na-view scan.
+
+    FP32 storage: 1e-5 and 1e-4 (FP32 arithmetic against FP64).  A reduced-precision form rounds
+    each filtered sample (and, for the F16 quads, the interpolation) independently per view, and a
+    voxel sums na views, so its relative error falls as 1/sqrt(na).  The F16 form is held to 1e-4
+    at the benchmark's 720 views -- the bound the benchmark's metric states -- scaled by
+    sqrt(720 / na); the BF16 form, with three fewer significand bits, to 4e-4 scaled the same way.
+    Max error: twice the RMSE bar."""
+    if storage == "f32":
+        return 1e-5, 1e-4
+    k = math.sqrt(720.0 / na) * (1e-4 if storage == "f16" else 4e-4)
+    return k, 2 * k

@@ -31,7 +31,7 @@ def _oracle_geom(rg):
                 na=rg.na, orbit=rg.orbit, orbit_start=rg.orbit_start, source_offset=0.0, dsd=rg.dsd, dod=rg.dod)
 
 
-@pytest.mark.parametrize("storage", ["f32", "bf16"])
+@pytest.mark.parametrize("storage", ["f32", "bf16", "f16"])
 def test_batch_equals_single_scan_plans(cuda, storage):
     rgs, igs = _scans()
     batch = S.FDKBatch(rgs, igs, storage=storage)
@@ -51,14 +51,20 @@ def test_batch_equals_single_scan_plans(cuda, storage):
             out = batch.get_output(i)
             single = S.fdk(S.plan_fbp(rg, ig, storage=storage), p)
             err = O.rel_rmse(out, single)
-            assert err < 1e-5, (i, rep, err)
+            # FP32 and BF16: the same arithmetic whatever the z-unroll.  F16 quads: the t-weights are
+            # rounded to a 2^-10 grid from the z-tile's first voxel, so a batch and a plan with
+            # different z-unrolls round them independently; they agree within half the form's own
+            # error bar against FP64 (test_batch_against_oracle holds each to the full bar)
+            bar = 0.5 * C.form_bars("f16", rg.na)[0] if storage == "f16" else 1e-5
+            assert err < bar, (i, rep, err)
             if ig.mask is not None:
                 assert np.all(out[~ig.mask] == 0)
 
 
-def test_batch_against_oracle(cuda):
+@pytest.mark.parametrize("storage", ["f32", "f16"])
+def test_batch_against_oracle(cuda, storage):
     rgs, igs = _scans()
-    batch = S.FDKBatch(rgs, igs)
+    batch = S.FDKBatch(rgs, igs, storage=storage)
     projs = [S.ellipsoid_proj(rg, C.ELL3) for rg in rgs]
     for i, p in enumerate(projs):
         batch.set_input(i, p)
@@ -66,8 +72,9 @@ def test_batch_against_oracle(cuda):
     for i, (rg, ig, p) in enumerate(zip(rgs, igs, projs)):
         ref = O.fdk(_oracle_geom(rg), dict(dims=ig.dims, deltas=ig.deltas, offsets=ig.offsets, mask=ig.mask), p)
         out = batch.get_output(i)
-        assert O.rel_rmse(out, ref) < 1e-5, i
-        assert np.abs(out - ref).max() <= 1e-4 * np.abs(ref).max(), i
+        rmse, maxrel = C.form_bars(storage, rg.na)
+        assert O.rel_rmse(out, ref) < rmse, i
+        assert np.abs(out - ref).max() <= maxrel * np.abs(ref).max(), i
 
 
 def test_batch_rejects_too_many_scans():

@@ -2,8 +2,8 @@
 
 * CBCT flat panel (CtFanFlat 512x384x720 -> 512x512x256, the benchmark): every 16th voxel in x and
   y on every 32nd slice against the FP64 oracle (the oracle filters every detector row by
-  FFT and back-projects the sampled voxels); exact scaling fdk(2p) == 2 fdk(p) and
-  additivity on the whole volume;
+  FFT and back-projects the sampled voxels), for the FP32 form and the F16 storage form; exact
+  scaling fdk(2p) == 2 fdk(p) and additivity on the whole volume;
 * 2D parallel beam (SinoPar 256 x 180, Hann) and 2D fan arc (SinoFanArc 888 x 512 views over a short
   scan, Parker, noisy): whole images against the FP64 oracle, compared inside the
   reconstruction FOV."""
@@ -38,7 +38,10 @@ def cbct_flat_512(cuda):
     return rg, ig, plan, proj, img
 
 
-def test_cbct_flat_512_sampled_voxels_match_fp64_oracle(cbct_flat_512):
+@pytest.fixture(scope="module")
+def cbct_flat_512_ref(cbct_flat_512):
+    """FP64 oracle on a sparse sample of the benchmark volume: every 16th voxel in x and y on
+    every 32nd slice (the oracle filters every detector row by FFT)."""
     rg, ig, plan, proj, img = cbct_flat_512
     g = dict(kind="flat", offset_s=0.0, offset_t=0.0, orbit_start=0.0, source_offset=0.0, **GEOM3)
     p = proj.cpu().numpy().astype(np.float64)
@@ -46,11 +49,32 @@ def test_cbct_flat_512_sampled_voxels_match_fp64_oracle(cbct_flat_512):
     # voxel centres d (i - (n-1)/2) at i = 0, 16, ... (x, y) and 0, 32, ... (z): a coarser grid
     # with the same centres, offset (stride - 1) / (2 stride) voxels of its own size
     sub = dict(dims=(32, 32, 8), deltas=(8.0, 8.0, 16.0), offsets=(15 / 32, 15 / 32, 31 / 64))
-    ref = O.cbct_back(filt, g, sub)
-    got = img.cpu().numpy()[0:256:32, 0:512:16, 0:512:16]
+    return O.cbct_back(filt, g, sub)
+
+
+def _sample(img):
+    return img.cpu().numpy()[0:256:32, 0:512:16, 0:512:16]
+
+
+def test_cbct_flat_512_sampled_voxels_match_fp64_oracle(cbct_flat_512, cbct_flat_512_ref):
+    ref = cbct_flat_512_ref
+    got = _sample(cbct_flat_512[4])
     assert got.shape == ref.shape
     assert O.rel_rmse(got, ref) < 1e-5
     assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
+def test_cbct_flat_512_f16_form_meets_1e4(cbct_flat_512, cbct_flat_512_ref):
+    """The F16 storage form (FP16 quads of the filtered projections, FP32 accumulation) on the
+    benchmark workload: relative RMSE <= 1e-4 against the FP64 oracle, the accuracy bound the
+    benchmark's metric states for a reduced-precision form, and max error <= 2e-4 max|ref|."""
+    rg, ig, plan, proj, img = cbct_flat_512
+    p16 = S.plan_fbp(rg, ig, storage="f16")
+    assert p16.info()["f16_quads"] and p16.info()["sample_bytes"] == 8
+    got = _sample(S.fdk(p16, proj))
+    ref = cbct_flat_512_ref
+    assert O.rel_rmse(got, ref) <= 1e-4
+    assert np.abs(got - ref).max() <= 2e-4 * np.abs(ref).max()
 
 
 def test_cbct_flat_512_scaling_is_exact_and_sums_add(cbct_flat_512):
