@@ -43,29 +43,39 @@ extern "C" {
 #define SGB_ERR_ARG 1         /* bad size / argument: reference throw("...") or error() */
 #define SGB_ERR_CUDA 2        /* CUDA runtime failure */
 #define SGB_ERR_NOMEM 3       /* device allocation failed */
-#define SGB_ERR_GEOM 4        /* impossible geometry (ramp.jl:217-219) */
+#define SGB_ERR_GEOM 4        /* impossible geometry (ramp.jl:70-72) */
 #define SGB_ERR_UNSUPPORTED 5 /* combination the reference also rejects */
 #define SGB_ERR_TIMEOUT 6     /* a bounded device-side wait gave up */
 
 /* flags */
 #define SGB_DEVICE_PTRS 1 /* bulk arrays are device pointers */
 #define SGB_ASYNC 2       /* do not synchronize the stream before returning */
+#define SGB_BDD_ARC 4     /* sgb_bdd_project / sgb_bdd_backproject: detector boundaries on the arc of
+                             radius DSD about the source (SinoFanArc).  No counterpart in the
+                             reference, whose distance-driven pair is flat-only (bdd_2d.jl:28-29) */
 
 /* geometry kinds: SinoPar, SinoFanArc/CtFanArc, SinoFanFlat/CtFanFlat */
 #define SGB_PAR 0
 #define SGB_ARC 1
 #define SGB_FLAT 2
 
-/* window shapes, window.jl:317-329 and WindowVect :279 */
+/* window shapes, window.jl:79-91 and WindowVect :41 */
 #define SGB_WIN_NONE 0
 #define SGB_WIN_BOXCAR 1
 #define SGB_WIN_HAMMING 2
 #define SGB_WIN_HANN 3
 #define SGB_WIN_VECT 4
 
-/* storage of the filtered projections inside fdk/fbp */
+/* storage of the filtered projections inside fdk/fbp (no counterpart in the reference, which
+ * keeps them in the input eltype, cbct-back.jl:166).  F32: FP32 (FP32 pairs (y, y[s+1] - y) for
+ * the TMA-staged back-projector).  BF16: BF16 samples.  F16: FP16 quads (y, y[t+1] - y,
+ * y[s+1] - y, mixed second difference) per detector sample, scaled by one power of two per
+ * call, interpolated in FP16 and accumulated in FP32; F16 plans whose quad boxes do not fit
+ * the TMA-staged back-projector, or with nt > 4096, use F32 storage (sgb_plan_info reports
+ * which). */
 #define SGB_STORE_F32 0
 #define SGB_STORE_BF16 1
+#define SGB_STORE_F16 2
 
 /* SinoPar / SinoFanArc / SinoFanFlat fields, src/geom/type2.jl:95-159 */
 typedef struct {
@@ -116,7 +126,7 @@ typedef struct {
     int npad;                  /* 0 = nextpow(2, n + 1) */
     int decon1;                /* default 1 */
     const double *filter;      /* optional user Hk of length npad (overrides the above) */
-    int storage;               /* SGB_STORE_F32 or SGB_STORE_BF16 */
+    int storage;               /* SGB_STORE_F32, SGB_STORE_BF16 or SGB_STORE_F16 (FDK plans) */
     int source_z;              /* FDK with a helical source: 0 ignores the source z as cbct_back does
                                   (cbct-back.jl:188-189); 1 back-projects t' = mag * (z - source_zs[view]),
                                   the line the reference leaves commented at cbct-back.jl:188 */
@@ -130,11 +140,14 @@ SGB_API int sgb_version(void);
 SGB_API int sgb_last_error(char *buf, size_t n);
 /* Number of CUDA kernels this library has launched since load (all threads). */
 SGB_API long long sgb_launch_count(void);
+/* Number of device allocations (cudaMalloc) this library has made since load (all threads).
+ * No counterpart in the reference. */
+SGB_API long long sgb_device_alloc_count(void);
 
 /* -------------------------------------------------- plan-time (host, FP64) */
-/* fbp_ramp / ramp_flat / ramp_arc, src/fbp/ramp.jl:171-238; kind SGB_PAR|SGB_FLAT = flat. */
+/* fbp_ramp / ramp_flat / ramp_arc, src/fbp/ramp.jl:24-91; kind SGB_PAR|SGB_FLAT = flat. */
 SGB_API int sgb_fbp_ramp(int kind, int N, double ds, double dsd, double *h);
-/* fbp_window, src/fbp/window.jl:298-312 (fftshift'ed, Float32-valued) */
+/* fbp_window, src/fbp/window.jl:60-74 (fftshift'ed, Float32-valued) */
 SGB_API int sgb_fbp_window(int shape, double cutoff, int N, const double *vect, double *win);
 /* _source_zs(rg), src/geom/ct-geom.jl:125-140: source z of each view (zeros for a circle) */
 SGB_API int sgb_source_zs(const sgb_ct_geom *rg, double *zs);
@@ -165,7 +178,7 @@ SGB_API int sgb_cbct_back(float *image, const float *proj, int ns, int nt, int n
                   int is_arc, const double *xc, const double *yc, const double *zc, int nx, int ny,
                   int nz, const uint8_t *mask, int ia_skip, int flags, void *stream);
 
-/* fbp_back_par!, src/fbp2/back-par.jl:360-407 (with fbp_back_par_xy :430-469).
+/* fbp_back_par!, src/fbp2/back-par.jl:206-253 (with fbp_back_par_xy :276-315).
  * sino (nb, na); sinphi/cosphi hold the ceil(na/ia_skip) views 1:ia_skip:na. */
 SGB_API int sgb_fbp_back_par(float *image, const float *sino, int nb, int na, const double *sinphi,
                      const double *cosphi, double ds, float offset, const double *xc,
@@ -191,9 +204,14 @@ SGB_API int sgb_bdd_project(const float *phantom, int nPix, int nDet, int na, co
  * vector, and the per-view scratch lives in a 16 MiB array inside the library that each
  * device holds until exit (requests needing more return SGB_ERR_ARG).  Nothing is
  * allocated.  The work is enqueued on `stream` and the call returns without waiting.
- * The first call on a device resolves the array's address and should come before any
- * stream capture; calls on one device share the array, so calls whose GPU work
- * overlaps race and must be serialised on one stream. */
+ * `angle` is copied to the device with cudaMemcpyAsync on `stream`: a pageable host vector
+ * may be reused as soon as the call returns, but a page-locked (pinned) one must stay
+ * unchanged until the stream has reached the call (a stream or event synchronisation).
+ * The first call on a device resolves the array's address (cudaGetSymbolAddress) and
+ * should come before any stream capture begins; the address is kept for the life of the
+ * process, so the entry point must not be used on a device after cudaDeviceReset.  Calls
+ * on one device share the array, so calls whose GPU work overlaps race and must be
+ * serialised on one stream. */
 SGB_API int sgb_bdd_project_noalloc(const float *phantom, int nPix, int nDet, int na,
                                     const double *angle, double DSD, double DS0, double pSize,
                                     double dSize, float *sino, void *stream);
@@ -214,6 +232,11 @@ SGB_API int sgb_bdd_backproject(const float *sino, int nPix, int nDet, int na, c
 typedef struct sgb_bdd_plan sgb_bdd_plan;
 SGB_API int sgb_bdd_plan_create(int nPix, int nDet, int na, const double *angle, double DSD, double DS0,
                                 double pSize, double dSize, sgb_bdd_plan **plan);
+/* The same with the detector shape: SGB_FLAT (the reference's pair) or SGB_ARC (boundaries on the
+ * arc of radius DSD about the source, at angles (k - nDet/2) dSize / DSD; no counterpart in the
+ * reference). */
+SGB_API int sgb_bdd_plan_create_det(int nPix, int nDet, int na, const double *angle, double DSD, double DS0,
+                                    double pSize, double dSize, int detector, sgb_bdd_plan **plan);
 SGB_API int sgb_bdd_plan_project(sgb_bdd_plan *plan, const float *phantom, float *sino, int flags,
                                  void *stream);
 SGB_API int sgb_bdd_plan_backproject(sgb_bdd_plan *plan, const float *sino, float *image, int flags,
@@ -221,8 +244,8 @@ SGB_API int sgb_bdd_plan_backproject(sgb_bdd_plan *plan, const float *sino, floa
 SGB_API int sgb_bdd_plan_destroy(sgb_bdd_plan *plan);
 
 /* Analytic line integrals standing in for ImagePhantoms.radon(rays(rg), ob) in the
- * reference tests (test/fbp2/fbp-fan.jl:106-109, test/fbp3/fdk.jl:23), with the ray
- * geometry of rays(rg) (sino-geom.jl:368-401, ct-geom.jl:227-239).
+ * reference tests (test/fbp2/fbp-fan.jl:14-25, test/fbp3/fdk.jl:23), with the ray
+ * geometry of rays(rg) (sino-geom.jl:99-132, ct-geom.jl:88-116).
  * ell rows: 2D (cx, cy, rx, ry, angle, density); 3D (cx, cy, cz, rx, ry, rz, phi, theta,
  * psi, density) with ZYZ Euler angles.  Output: sino (nb, na) / proj (ns, nt, na). */
 SGB_API int sgb_ellipse_sino(const sgb_sino_geom *rg, const double *ell, int nell, float *sino, int flags,
@@ -270,7 +293,8 @@ SGB_API int sgb_plan_last_timing(sgb_plan *plan, double *ms, int n);
  * back-projection uses the TMA-staged kernel, info[1..2] = staged box (samples),
  * info[3] = row pitch of the filtered projections, info[4] = voxels per thread along z,
  * info[5] (when n >= 6) = launches the views are split over, info[6] (when n >= 7) = bytes per
- * stored filtered sample (8: FP32 pairs (y, y[next] - y), 4: FP32, 2: BF16). */
+ * stored filtered sample (8: FP32 pairs (y, y[next] - y) or FP16 quads, 4: FP32, 2: BF16),
+ * info[7] (when n >= 8) = 1 when the 8-byte samples are FP16 quads (F16 storage). */
 SGB_API int sgb_plan_info(const sgb_plan *plan, int *info, int n);
 /* Overrides the autotuner's choice of how many launches an FDK plan splits its views over (the
  * later launches add to the volume); 1 <= passes <= min(8, na).  Results agree to rounding. */
@@ -321,7 +345,7 @@ SGB_API int sgb_selftest_wait_timeout(long long budget_cycles, void *stream);
  * image's radial FOV exceeds 0.99 dso. */
 SGB_API int sgb_footprint_size_sino(const sgb_sino_geom *rg, const sgb_image_geom *ig, float *size);
 SGB_API int sgb_footprint_size_ct(const sgb_ct_geom *rg, const sgb_image_geom *ig, float *size);
-/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59: Radon transform of the
+/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-58: Radon transform of the
  * Zwart-Powell box spline at radius r (pixel units) and angle phi (host, FP64). */
 SGB_API double sgb_zwart_powell(double r, double phi);
 /* out[i + nr*j] = zwart_powell(r[i], phi[j]) for a grid of radii and angles (the

@@ -48,10 +48,10 @@ int orc_num_threads(void) {
 
 /* ------------------------------------------------------------------ ramp.jl */
 
-/* _ramp_flat, src/fbp/ramp.jl:199-205 and ramp_flat :233-238.
+/* _ramp_flat, src/fbp/ramp.jl:52-58 and ramp_flat :86-91.
  * h[m] for n = m - N/2, n = -(N/2):(N/2-1). */
 int orc_ramp_flat(int N, double ds, double *h) {
-    if (N % 2) return ORC_ERR_ARG; /* ramp.jl:234 "N must be even" */
+    if (N % 2) return ORC_ERR_ARG; /* ramp.jl:87 "N must be even" */
     for (int m = 0; m < N; m++) {
         int n = m - N / 2;
         double v;
@@ -63,10 +63,10 @@ int orc_ramp_flat(int N, double ds, double *h) {
     return ORC_OK;
 }
 
-/* _ramp_arc, src/fbp/ramp.jl:191-197 and ramp_arc :214-224. */
+/* _ramp_arc, src/fbp/ramp.jl:44-50 and ramp_arc :67-77. */
 int orc_ramp_arc(int N, double ds, double dsd, double *h) {
-    if (N % 2) return ORC_ERR_ARG;                            /* ramp.jl:215 */
-    if (N / 2.0 * ds / dsd > 0.9 * PI / 2) return ORC_ERR_GEOM; /* ramp.jl:217-219 */
+    if (N % 2) return ORC_ERR_ARG;                            /* ramp.jl:68 */
+    if (N / 2.0 * ds / dsd > 0.9 * PI / 2) return ORC_ERR_GEOM; /* ramp.jl:70-72 */
     for (int m = 0; m < N; m++) {
         int n = m - N / 2;
         double v;
@@ -80,7 +80,7 @@ int orc_ramp_arc(int N, double ds, double dsd, double *h) {
 
 /* ---------------------------------------------------------------- window.jl */
 
-/* fbp_window, src/fbp/window.jl:298-312 plus the shapes :317-329.
+/* fbp_window, src/fbp/window.jl:60-74 plus the shapes :79-91.
  * shape: 0 NoWindow, 1 Boxcar, 2 Hamming, 3 Hann, 4 WindowVect (vect given).
  * The reference stores the window as Float32 (T = Float32 default, :298), so values
  * are rounded through float before use.  Output is fftshift'ed (:302). */
@@ -312,7 +312,7 @@ int orc_cbct_back_zs(real_t *image, const real_t *proj, int ns, int nt, int na, 
             real_t x_beta = x_ds * c_b + y_ds * s_b;              /* :174 */
             real_t y_beta = dso_ds - (-x_ds * s_b + y_ds * c_b);   /* :175 */
             real_t mag, sprime_ds, w2;
-            if (is_arc == 2) { /* CtPar: the source at infinity, t' = z, unit weight (back-par.jl:447 in 3D) */
+            if (is_arc == 2) { /* CtPar: the source at infinity, t' = z, unit weight (back-par.jl:293 in 3D) */
                 mag = 1;
                 sprime_ds = x_beta;
                 w2 = 1;
@@ -355,7 +355,7 @@ int orc_cbct_back(real_t *image, const real_t *proj, int ns, int nt, int na, con
 
 /* ------------------------------------------------------------- back-par.jl */
 
-/* fbp_back_par! + fbp_back_par_xy, src/fbp2/back-par.jl:360-469.
+/* fbp_back_par! + fbp_back_par_xy, src/fbp2/back-par.jl:206-315.
  * sino (nb, na); sinphi/cosphi hold the ceil(na/ia_skip) subsampled views (:326-327). */
 int orc_back_par(real_t *image, const real_t *sino, int nb, int na, const double *sinphi,
                  const double *cosphi, double ds, float offset, const double *xc, const double *yc,
@@ -449,15 +449,23 @@ static double interp_flat(const double *k, const double *v, int n, double xq) {
 
 /* Shared per-view set-up of project_bdd / backproject_bdd (bdd_2d.jl:28-35, 45-86,
  * 130-187).  Fills detm (nDet+1), L (nDet) and, per "row" r, the mapped boundaries
- * rowm(r, 0..nPix) via a callback-free formula; returns axisCase. */
+ * rowm(r, 0..nPix) via a callback-free formula; returns axisCase.
+ * arc = 1 (no counterpart in the reference, which is flat-only): detector boundary k lies on
+ * the circle of radius DSD about the source, at angle (k - nDet/2) dSize / DSD from the
+ * central ray, i.e. at (DSD sin g, DS0 - DSD cos g) before the view rotation. */
 static int bdd_view_setup(double beta, int nPix, int nDet, double DSD, double DS0, double pSize,
-                          double dSize, double *detm, double *L, double *rtx, double *rty) {
+                          double dSize, int arc, double *detm, double *L, double *rtx, double *rty) {
     double rtubeX = -DS0 * sin(beta), rtubeY = DS0 * cos(beta);           /* :45-46 */
     int axisCase = !(((beta >= PI / 4) && (beta <= 3 * PI / 4)) ||
                      ((beta >= 5 * PI / 4) && (beta <= 7 * PI / 4)));     /* :53-57 */
-    double detY = -(DSD - DS0) - (dSize / 2);                            /* :29 */
     for (int k = 0; k <= nDet; k++) {
         double detX = (-(nDet / 2.0) + k) * dSize;                        /* :28 */
+        double detY = -(DSD - DS0) - (dSize / 2);                          /* :29 */
+        if (arc) {
+            double g = (-(nDet / 2.0) + k) * dSize / DSD;
+            detX = DSD * sin(g);
+            detY = DS0 - DSD * cos(g);
+        }
         double rdX = detX * cos(beta) - detY * sin(beta);                  /* :49 */
         double rdY = detX * sin(beta) + detY * cos(beta);                  /* :50 */
         detm[k] = axisCase ? map2x(rtubeX, rtubeY, rdX, rdY) : map2y(rtubeX, rtubeY, rdX, rdY);
@@ -497,8 +505,8 @@ static void bdd_rowm(int axisCase, int r, int nPix, double pSize, double rtx, do
 
 /* project_bdd, src/sys2/bdd_2d.jl:17-110.  phantom (nPix, nPix) column-major with
  * row = y (row 1 = top), col = x; sino (na, nDet) column-major (angle fastest). */
-int orc_bdd_project(const real_t *phantom, int nPix, int nDet, int na, const double *angle,
-                    double DSD, double DS0, double pSize, double dSize, real_t *sino) {
+int orc_bdd_project_det(const real_t *phantom, int nPix, int nDet, int na, const double *angle,
+                        double DSD, double DS0, double pSize, double dSize, int arc, real_t *sino) {
 #pragma omp parallel for schedule(dynamic, 1)
     for (int p = 0; p < na; p++) {
         double *detm = (double *)malloc(sizeof(double) * (nDet + 1));
@@ -508,7 +516,7 @@ int orc_bdd_project(const real_t *phantom, int nPix, int nDet, int na, const dou
         double *Pdk = (double *)malloc(sizeof(double) * (nDet + 1));
         double *acc = (double *)calloc(nDet, sizeof(double));
         double rtx, rty;
-        int axisCase = bdd_view_setup(angle[p], nPix, nDet, DSD, DS0, pSize, dSize, detm, L, &rtx, &rty);
+        int axisCase = bdd_view_setup(angle[p], nPix, nDet, DSD, DS0, pSize, dSize, arc, detm, L, &rtx, &rty);
         for (int r = 0; r < nPix; r++) {                                   /* :91 */
             bdd_rowm(axisCase, r, nPix, pSize, rtx, rty, rowm);
             /* img row: x-case phantom[r, :]; y-case reverse(phantom', 2)[r, c] = phantom[nPix-1-c, r] */
@@ -531,8 +539,8 @@ int orc_bdd_project(const real_t *phantom, int nPix, int nDet, int na, const dou
 /* backproject_bdd, src/sys2/bdd_2d.jl:119-220, including the aliasing of reconImgTmp
  * with the initial reconImg (:139-140): the first view's un-transposed row block is
  * added once more on top of the regular sum. */
-int orc_bdd_back(const real_t *sino, int nPix, int nDet, int na, const double *angle, double DSD,
-                 double DS0, double pSize, double dSize, real_t *image) {
+int orc_bdd_back_det(const real_t *sino, int nPix, int nDet, int na, const double *angle, double DSD,
+                     double DS0, double pSize, double dSize, int arc, real_t *image) {
     long npix2 = (long)nPix * nPix;
     int nth = orc_num_threads();
     double *part = (double *)calloc((size_t)nth * npix2, sizeof(double));
@@ -554,7 +562,7 @@ int orc_bdd_back(const real_t *sino, int nPix, int nDet, int na, const double *a
 #pragma omp for schedule(dynamic, 1)
         for (int p = 0; p < na; p++) {
             double rtx, rty;
-            int axisCase = bdd_view_setup(angle[p], nPix, nDet, DSD, DS0, pSize, dSize, detm, L, &rtx, &rty);
+            int axisCase = bdd_view_setup(angle[p], nPix, nDet, DSD, DS0, pSize, dSize, arc, detm, L, &rtx, &rty);
             real_t Px = 0;                                                   /* :196 */
             Ppj[0] = 0;
             for (int n = 0; n < nDet; n++) {
@@ -588,10 +596,20 @@ int orc_bdd_back(const real_t *sino, int nPix, int nDet, int na, const double *a
     return ORC_OK;
 }
 
+/* The reference's flat-detector pair (bdd_2d.jl:17-110, 119-220). */
+int orc_bdd_project(const real_t *phantom, int nPix, int nDet, int na, const double *angle,
+                    double DSD, double DS0, double pSize, double dSize, real_t *sino) {
+    return orc_bdd_project_det(phantom, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, 0, sino);
+}
+int orc_bdd_back(const real_t *sino, int nPix, int nDet, int na, const double *angle, double DSD,
+                 double DS0, double pSize, double dSize, real_t *image) {
+    return orc_bdd_back_det(sino, nPix, nDet, na, angle, DSD, DS0, pSize, dSize, 0, image);
+}
+
 /* ------------------------------------------------ analytic phantom projections */
 
 /* Line integrals of ellipses in parallel-beam coordinates (r, phi), the role played by
- * ImagePhantoms.radon in the reference tests (test/fbp2/fbp-fan.jl:106-109).
+ * ImagePhantoms.radon in the reference tests (test/fbp2/fbp-fan.jl:14-25).
  * ell: nell x 6 rows (cx, cy, rx, ry, angle, density). */
 void orc_ellipse_radon(const double *ell, int nell, const double *r, const double *phi, long n,
                        double *out) {
@@ -639,7 +657,7 @@ static double ellipsoid_chord(const double *E, const double *src, const double *
 }
 
 /* Cone-beam projections of ellipsoids for CtFanArc / CtFanFlat, using the detector
- * geometry of src/fbp3/cb_arc_to_par.jl:23-43 and cb_flat_to_par.jl:66-73 (source at
+ * geometry of src/fbp3/cb_arc_to_par.jl:23-43 and cb_flat_to_par.jl:23-30 (source at
  * (-dso sin b, dso cos b, 0), detector s-axis (cos b, sin b, 0), t along z).
  * ell: nell x 10 rows (cx, cy, cz, rx, ry, rz, phi, theta, psi, density).
  * s (ns), t (nt), betas (na) -> proj (ns, nt, na). */
@@ -668,7 +686,7 @@ void orc_ellipsoid_cone(const double *ell, int nell, int is_arc, const double *s
 
 
 /* ---------------------------------------------------------------- sys2 */
-/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59 (always FP64, like the reference's
+/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-58 (always FP64, like the reference's
  * Float64 call).  BoxSp_k is written as the sum over the 2^m signed corners of the
  * active directions (the same central differences, expanded). */
 static double orc_zp0(double y, int n) { return y > 0 ? pow(y, n - 1) : 0.0; }

@@ -47,7 +47,8 @@ def lib(bits: int = 64) -> ctypes.CDLL:
         L = ctypes.CDLL(path)
         for name in ("orc_ramp_flat", "orc_ramp_arc", "orc_window", "orc_fbp_filter", "orc_sino_filter",
                      "orc_angle_weight", "orc_parker_par", "orc_parker_fan_short", "orc_cbct_back",
-                     "orc_back_par", "orc_back_fan", "orc_bdd_project", "orc_bdd_back", "orc_real_bytes",
+                     "orc_back_par", "orc_back_fan", "orc_bdd_project", "orc_bdd_back", "orc_bdd_project_det",
+                     "orc_bdd_back_det", "orc_real_bytes",
                      "orc_num_threads"):
             getattr(L, name).restype = _c_int
         _LIBS[bits] = L
@@ -70,10 +71,10 @@ def _check(rc, what):
 
 
 # ------------------------------------------------------------------ geometry scalars
-# src/geom/common.jl:27-99, sino-geom.jl:287-295, ct-geom.jl:148-152
+# src/geom/common.jl:27-99, sino-geom.jl:18-26, ct-geom.jl:19-23
 
 def ar(g) -> np.ndarray:
-    """_ar: angles in radians, common.jl:27-34 + unit.jl:161."""
+    """_ar: angles in radians, common.jl:27-34 + unit.jl:10."""
     na, orbit, start = int(_f(g, "na")), float(_f(g, "orbit")), float(_f(g, "orbit_start", 0.0))
     return (start + np.arange(na) * (orbit / na)) * (math.pi / 180)
 
@@ -88,7 +89,7 @@ def is_ct(g) -> bool:
 
 
 def s_axis(g) -> np.ndarray:
-    """_s: sino-geom.jl:287-289 / ct-geom.jl:148-151."""
+    """_s: sino-geom.jl:18-20 / ct-geom.jl:19-23."""
     if is_ct(g):
         n, d, off = int(_f(g, "ns")), float(_f(g, "ds")), float(np.float32(_f(g, "offset_s", 0.0)))
     else:
@@ -143,7 +144,7 @@ def _mask(ig):
 # ------------------------------------------------------------ filter / weights
 
 def ramp(g, N: int) -> np.ndarray:
-    """fbp_ramp, ramp.jl:171-182."""
+    """fbp_ramp, ramp.jl:24-35."""
     h = np.zeros(N)
     d = float(_f(g, "ds")) if is_ct(g) else float(_f(g, "d"))
     if _f(g, "kind") == "arc":
@@ -334,9 +335,11 @@ def fbp(g, ig, sino: np.ndarray, shape="none", cutoff=1.0, npad=None, decon1=Tru
 
 # --------------------------------------------------------------------- bdd_2d.jl
 
-def bdd_geo(DSD, DS0, pSize, dSize, nPix, nDet, angle):
+def bdd_geo(DSD, DS0, pSize, dSize, nPix, nDet, angle, arc=False):
+    """The reference's geo tuple; arc=True puts the detector boundaries on the arc of radius DSD
+    about the source (an extension: the reference pair is flat-only)."""
     return dict(DSD=float(DSD), DS0=float(DS0), pSize=float(pSize), dSize=float(dSize), nPix=int(nPix),
-                nDet=int(nDet), angle=np.ascontiguousarray(angle, dtype=np.float64))
+                nDet=int(nDet), angle=np.ascontiguousarray(angle, dtype=np.float64), arc=bool(arc))
 
 
 def project_bdd(phantom: np.ndarray, geo, bits: int = 64) -> np.ndarray:
@@ -346,9 +349,10 @@ def project_bdd(phantom: np.ndarray, geo, bits: int = 64) -> np.ndarray:
     ph = np.ascontiguousarray(phantom, dtype=dt_)
     na = len(geo["angle"])
     out = np.zeros((geo["nDet"], na), dtype=dt_)
-    _check(lib(bits).orc_bdd_project(_ptr(ph), geo["nPix"], geo["nDet"], na, _ptr(geo["angle"]),
-                                     _c_double(geo["DSD"]), _c_double(geo["DS0"]), _c_double(geo["pSize"]),
-                                     _c_double(geo["dSize"]), _ptr(out)), "bdd_project")
+    _check(lib(bits).orc_bdd_project_det(_ptr(ph), geo["nPix"], geo["nDet"], na, _ptr(geo["angle"]),
+                                         _c_double(geo["DSD"]), _c_double(geo["DS0"]), _c_double(geo["pSize"]),
+                                         _c_double(geo["dSize"]), int(geo.get("arc", False)), _ptr(out)),
+           "bdd_project")
     return out
 
 
@@ -358,9 +362,10 @@ def backproject_bdd(sino: np.ndarray, geo, bits: int = 64) -> np.ndarray:
     s = np.ascontiguousarray(sino, dtype=dt_)
     na = len(geo["angle"])
     out = np.zeros((geo["nPix"], geo["nPix"]), dtype=dt_)
-    _check(lib(bits).orc_bdd_back(_ptr(s), geo["nPix"], geo["nDet"], na, _ptr(geo["angle"]),
-                                  _c_double(geo["DSD"]), _c_double(geo["DS0"]), _c_double(geo["pSize"]),
-                                  _c_double(geo["dSize"]), _ptr(out)), "bdd_back")
+    _check(lib(bits).orc_bdd_back_det(_ptr(s), geo["nPix"], geo["nDet"], na, _ptr(geo["angle"]),
+                                      _c_double(geo["DSD"]), _c_double(geo["DS0"]), _c_double(geo["pSize"]),
+                                      _c_double(geo["dSize"]), int(geo.get("arc", False)), _ptr(out)),
+           "bdd_back")
     return out
 
 
@@ -377,7 +382,7 @@ def ellipse_radon(ell: np.ndarray, r: np.ndarray, phi: np.ndarray) -> np.ndarray
 
 
 def sino_rays(g):
-    """rays(rg) for 2D geometries (sino-geom.jl:368-401) -> (r, phi), numpy (na, nb)."""
+    """rays(rg) for 2D geometries (sino-geom.jl:99-132) -> (r, phi), numpy (na, nb)."""
     s, b = s_axis(g), ar(g)
     if _f(g, "kind") == "par":
         return np.broadcast_to(s[None, :], (len(b), len(s))), np.broadcast_to(b[:, None], (len(b), len(s)))
@@ -391,12 +396,19 @@ def ellipse_sino(g, ell) -> np.ndarray:
     return ellipse_radon(ell, r, phi)
 
 
-def ellipsoid_proj(rg, ell) -> np.ndarray:
+def ellipsoid_proj(rg, ell, rows=None) -> np.ndarray:
+    """Cone-beam line integrals of ellipsoids, (na, nt, ns).  `rows` (detector row indices)
+    limits the work to those rows; the others stay zero."""
     ell = np.ascontiguousarray(ell, dtype=np.float64).reshape(-1, 10)
     s, t, b = (np.ascontiguousarray(v) for v in (s_axis(rg), t_axis(rg), ar(rg)))
+    ts = t if rows is None else np.ascontiguousarray(t[np.asarray(rows)])
+    part = np.zeros((len(b), len(ts), len(s)))
+    lib().orc_ellipsoid_cone(_ptr(ell), len(ell), int(_f(rg, "kind") == "arc"), _ptr(s), len(s), _ptr(ts), len(ts),
+                             _ptr(b), len(b), _c_double(dso(rg)), _c_double(float(_f(rg, "dsd"))), _ptr(part))
+    if rows is None:
+        return part
     out = np.zeros((len(b), len(t), len(s)))
-    lib().orc_ellipsoid_cone(_ptr(ell), len(ell), int(_f(rg, "kind") == "arc"), _ptr(s), len(s), _ptr(t), len(t),
-                             _ptr(b), len(b), _c_double(dso(rg)), _c_double(float(_f(rg, "dsd"))), _ptr(out))
+    out[:, np.asarray(rows), :] = part
     return out
 
 
@@ -424,7 +436,7 @@ def sino_filter_fft(x: np.ndarray, Hk: np.ndarray, workers: int = 1, chunk_rows:
 
 # ---------------------------------------------------------------- sys2
 def zwart_powell(r, phi):
-    """zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-59 (C restatement, FP64)."""
+    """zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-58 (C restatement, FP64)."""
     f = lib(64).orc_zwart_powell
     f.restype = ctypes.c_double
     f.argtypes = [ctypes.c_double, ctypes.c_double]

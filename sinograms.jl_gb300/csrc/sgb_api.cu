@@ -91,6 +91,9 @@ struct sgb_plan {
     float scale = 1.f;
     // staging for host-pointer calls
     DevBuf in_buf, filt_buf, img_buf;
+    // F16 form: the filter's FP32 rows before they become FP16 quads, and the device words
+    // (max |y| as bits, inverse scale) of the quads' power-of-two scale
+    DevBuf qtmp, qword;
     // FDK back-projection: pitched filtered buffer and the TMA-staged kernel's set-up
     int pitch = 0;
     bool tma = false;
@@ -134,6 +137,8 @@ int plan_common(sgb_plan *P, int kind, int ndet, double d, double dsd, const sgb
     o.cutoff = 1.0;
     o.decon1 = 1;
     if (opt) o = *opt;
+    SGB_REQUIRE(o.storage == SGB_STORE_F32 || o.storage == SGB_STORE_BF16 || o.storage == SGB_STORE_F16,
+                "plan_fbp: unknown storage form %d", o.storage);
     P->storage = o.storage;
     P->ndet = ndet;
     P->nrow = nrow;
@@ -194,7 +199,7 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
     FdkTmaArgs &A = P->targs;
     TuneKey key;
     memset(&key, 0, sizeof key);
-    key = TuneKey{g.kind, g.ns, g.nt, g.na, P->nx, P->ny, P->nz, A.elem_bytes, (float)g.dsd, (float)(g.dsd - g.dod),
+    key = TuneKey{g.kind, g.ns, g.nt, g.na, P->nx, P->ny, P->nz, A.elem_bytes * 2 + A.quad, (float)g.dsd, (float)(g.dsd - g.dod),
                   (float)g.ds, (float)g.dt, A.dx, A.dy, A.dz};
     // a candidate is (voxels per thread along z, launches the views are split over), coded zu * 4 + passes
     int best = 0;
@@ -302,8 +307,9 @@ int fdk_tma_autotune(sgb_plan *P, cudaStream_t st, bool tune) {
 // Filtered-projection layout and back-projector choice for an FDK plan: rows padded to
 // a multiple of 8 samples (16-byte TMA strides for every storage type); the TMA-staged
 // kernel when its box fits (exhaustive pre-pass), the direct kernel otherwise.  FP32 storage
-// for the TMA-staged kernel holds pairs (y, y[next] - y), 8 bytes per sample; the direct
-// kernel reads plain FP32 samples.
+// for the TMA-staged kernel holds pairs (y, y[next] - y), 8 bytes per sample, and F16 storage
+// FP16 quads, also 8 bytes; the direct kernel reads plain FP32 samples (F16 plans whose quad
+// boxes do not fit fall back to FP32 storage).
 int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool tune) {
     const sgb_ct_geom &g = P->cg;
     const int elem = P->storage == SGB_STORE_BF16 ? 2 : 8;
@@ -311,6 +317,16 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     SGB_TRY(P->filt_buf.reserve((size_t)P->pitch * g.nt * g.na * elem));
     SGB_CUDA(cudaMemsetAsync(P->filt_buf.p, 0, (size_t)P->pitch * g.nt * g.na * elem, st));
     FdkTmaArgs &A = P->targs;
+    // FP16 quads need nt <= 4096 (their t-weights come from a 2^-10 grid, sgb_fdk_tma_dev.cuh);
+    // taller detectors keep FP32 storage
+    A.quad = P->storage == SGB_STORE_F16 && g.nt <= 4096;
+    A.qscale = nullptr;
+    if (A.quad) {  // inverse scale 1 until the first call packs quads
+        const float w[2] = {0.f, 1.f};
+        SGB_TRY(P->qword.reserve(sizeof w));
+        SGB_CUDA(cudaMemcpy(P->qword.p, w, sizeof w, cudaMemcpyHostToDevice));
+        A.qscale = P->qword.as<float>() + 1;
+    }
     A.trig = P->trig.as<float2>();
     A.zsrc = P->zsrc.p ? P->zsrc.as<float>() : nullptr;
     A.ns = g.ns;
@@ -347,12 +363,17 @@ int plan_fdk_back(sgb_plan *P, const sgb_image_geom *ig, cudaStream_t st, bool t
     P->tma = false;
     if (std::sqrt(rx * rx + ry * ry) < 0.9 * (g.dsd - g.dod)) {
         SGB_TRY(fdk_tma_autotune(P, st, tune));
-        if (!P->tma && A.elem_bytes == 8) {  // pair boxes too large: plain FP32 boxes
+        if (!P->tma && A.elem_bytes == 8) {  // pair or quad boxes too large: plain FP32 boxes
             A.elem_bytes = 4;
+            A.quad = 0;
             SGB_TRY(fdk_tma_autotune(P, st, tune));
         }
     }
-    if (!P->tma && A.elem_bytes == 8) A.elem_bytes = 4;  // direct kernel: plain FP32 rows
+    if (!P->tma && A.elem_bytes == 8) {  // direct kernel: plain FP32 rows
+        A.elem_bytes = 4;
+        A.quad = 0;
+    }
+    if (A.quad) SGB_TRY(P->qtmp.reserve((size_t)P->pitch * g.nt * g.na * sizeof(float)));
     return SGB_OK;
 }
 
@@ -532,6 +553,7 @@ int sgb_plan_info(const sgb_plan *P, int *info, int n) {
     info[4] = P->targs.zu;
     if (n >= 6) info[5] = P->targs.passes;
     if (n >= 7) info[6] = P->ct ? P->targs.elem_bytes : 4;
+    if (n >= 8) info[7] = P->ct ? P->targs.quad : 0;
     return SGB_OK;
 }
 
@@ -573,10 +595,21 @@ static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *o
     A.sBt = P->sBt;
     A.scale = P->scale;
     A.err = P->filt_err;
-    const int kind = P->storage == SGB_STORE_BF16 ? FILTER_OUT_BF16
-                                                  : (P->ct && P->tma && P->targs.elem_bytes == 8 ? FILTER_OUT_PAIR
-                                                                                                 : FILTER_OUT_F32);
+    // FP32 pairs for the pair boxes; F16 plans filter to FP32 rows that become quads afterwards
+    const bool pairs = P->ct && P->tma && P->targs.elem_bytes == 8 && !P->targs.quad;
+    const int kind = P->storage == SGB_STORE_BF16 ? FILTER_OUT_BF16 : (pairs ? FILTER_OUT_PAIR : FILTER_OUT_F32);
     return launch_filter_rows(A, P->filt, P->split_shared ? *P->split_shared : P->split, out, kind, st);
+}
+
+// The weighted ramp filter of an FDK plan into its filtered buffer: FP32 pairs, FP32 or BF16 rows
+// straight from the filter, or (F16 form) FP32 rows packed into FP16 quads.
+static int filter_projections(sgb_plan *P, const float *in_dev, cudaStream_t st) {
+    const sgb_ct_geom &g = P->cg;
+    const long long rows = (long long)g.nt * g.na;
+    if (!(P->tma && P->targs.quad)) return run_filter(P, in_dev, rows, P->filt_buf.p, st, P->pitch);
+    SGB_TRY(run_filter(P, in_dev, rows, P->qtmp.p, st, P->pitch));
+    return launch_quad_pack(P->qtmp.as<float>(), P->pitch, g.ns, g.nt, rows, P->filt_buf.p, P->qword.as<unsigned>(),
+                            P->qword.as<float>() + 1, st);
 }
 
 int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *stream) {
@@ -589,8 +622,7 @@ int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *strea
     SGB_TRY(stage_in(proj, nproj * sizeof(float), flags, P->in_buf, &in_dev, st));
     // step 1+2: view weights fused into the ramp filter (fdk.jl:72-75), rows padded to pitch
     P->mark(0, st);
-    SGB_TRY(run_filter(P, static_cast<const float *>(in_dev), (long long)g.nt * g.na, P->filt_buf.p, st,
-                       P->pitch));
+    SGB_TRY(filter_projections(P, static_cast<const float *>(in_dev), st));
     P->mark(1, st);
     float *img_dev = image;
     if (!(flags & SGB_DEVICE_PTRS)) {
@@ -888,7 +920,7 @@ static int back2_seam(float *image, const float *sino, int nb, int na, const dou
     A.nv = nv;
     A.ia_skip = ia_skip;
     A.nslices = 1;
-    A.wb = (float)((nb + 1) / 2.0 + offset);  // back-par.jl:378, back-fan.jl:236
+    A.wb = (float)((nb + 1) / 2.0 + offset);  // back-par.jl:224, back-fan.jl:236
     A.mode = mode;
     A.dsd_ds = (float)(dsd / ds);
     A.dso_ds = (float)(dso / ds);
@@ -924,7 +956,7 @@ static int bdd_seam(bool forward, const float *in, int nPix, int nDet, int na, c
     cudaStream_t st = as_stream(stream);
     DevBuf dang, scratch, din, dout;
     SGB_TRY(upload_f64(angle, na, dang, st));
-    BddArgs G{nPix, nDet, na, dang.as<double>(), DSD, DS0, pSize, dSize};
+    BddArgs G{nPix, nDet, na, dang.as<double>(), DSD, DS0, pSize, dSize, (flags & SGB_BDD_ARC) ? 1 : 0};
     SGB_TRY(scratch.reserve(forward ? bdd_project_scratch(G) : bdd_back_scratch(G)));
     size_t nin = forward ? (size_t)nPix * nPix : (size_t)na * nDet;
     size_t nout = forward ? (size_t)na * nDet : (size_t)nPix * nPix;
@@ -971,13 +1003,19 @@ extern "C" {
 
 int sgb_bdd_plan_create(int nPix, int nDet, int na, const double *angle, double DSD, double DS0, double pSize,
                         double dSize, sgb_bdd_plan **out) {
+    return sgb_bdd_plan_create_det(nPix, nDet, na, angle, DSD, DS0, pSize, dSize, SGB_FLAT, out);
+}
+
+int sgb_bdd_plan_create_det(int nPix, int nDet, int na, const double *angle, double DSD, double DS0,
+                            double pSize, double dSize, int detector, sgb_bdd_plan **out) {
     SGB_REQUIRE(out && angle, "bdd_plan_create: null argument");
     SGB_REQUIRE(nPix > 0 && nDet > 0 && na > 0, "bdd_plan_create: sizes must be positive");
+    SGB_REQUIRE(detector == SGB_FLAT || detector == SGB_ARC, "bdd_plan_create: detector must be SGB_FLAT or SGB_ARC");
     *out = nullptr;
     auto P = std::make_unique<sgb_bdd_plan>();
     cudaStream_t st = nullptr;
     SGB_TRY(upload_f64(angle, na, P->angle, st));
-    P->G = BddArgs{nPix, nDet, na, P->angle.as<double>(), DSD, DS0, pSize, dSize};
+    P->G = BddArgs{nPix, nDet, na, P->angle.as<double>(), DSD, DS0, pSize, dSize, detector == SGB_ARC ? 1 : 0};
     SGB_TRY(P->fwd.reserve(bdd_project_scratch(P->G)));
     SGB_TRY(P->back.reserve(bdd_back_scratch(P->G)));
     SGB_TRY(launch_bdd_project_setup(P->G, P->fwd.p, st));
@@ -1112,13 +1150,17 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     SGB_CUDA(cudaGetDevice(&dev));
     SGB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     std::vector<size_t> class_begin;
-    for (int ecls : {8, 4, 2}) {  // element size: FP32 pairs, FP32, BF16
+    // sample form: FP32 pairs, FP16 quads (8 bytes), FP32, BF16
+    const int2 forms[4] = {make_int2(8, 0), make_int2(8, 1), make_int2(4, 0), make_int2(2, 0)};
+    for (const int2 form : forms) {
+        const int ecls = form.x, quad = form.y;
         for (int cls = 0; cls < 18; cls++) {  // box width 32/64/128 x ZU 16/32/64 x ring of 4 or 2 stages
             const int W = 32 << (cls % 3), zu = 16 << ((cls / 3) % 3), ns = cls < 9 ? kNStageDefault : 2;
             std::vector<int> order;
             int box_bytes = 0;
             for (int i = 0; i < n; i++)
-                if (scans[i].W == W && scans[i].elem_bytes == ecls && scans[i].zu == zu && scans[i].nstage == ns) {
+                if (scans[i].W == W && scans[i].elem_bytes == ecls && scans[i].quad == quad && scans[i].zu == zu &&
+                    scans[i].nstage == ns) {
                     order.push_back(i);
                     box_bytes = std::max(box_bytes, scans[i].box_bytes);
                 }
@@ -1131,6 +1173,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
             C.zu = zu;
             C.box_bytes = box_bytes;
             C.elem_bytes = elem;
+            C.quad = quad;
             C.nstage = ns;
             // views per stage: the most resident CTAs per SM first (the kernel is issue-bound, so
             // two CTAs of 9 warps beat one CTA with a deeper ring), then the most views per stage;
@@ -1184,7 +1227,7 @@ int batch_build(sgb_batch *B, int n, const sgb_ct_geom *rgs, const sgb_image_geo
     if (cudaEventRecordWithFlags(B->ev[0], B->capture, cudaEventRecordExternal) != cudaSuccess) s = SGB_ERR_CUDA;
     for (int i = 0; i < n && s == SGB_OK; i++) {
         sgb_plan *P = B->plans[i];
-        s = run_filter(P, P->in_buf.as<float>(), (long long)P->cg.nt * P->cg.na, P->filt_buf.p, B->capture, P->pitch);
+        s = filter_projections(P, P->in_buf.as<float>(), B->capture);
     }
     if (s == SGB_OK && cudaMemsetAsync(B->counter.p, 0, kMaxBatchClasses * sizeof(int), B->capture) != cudaSuccess) s = SGB_ERR_CUDA;
     if (s == SGB_OK && cudaEventRecordWithFlags(B->ev[1], B->capture, cudaEventRecordExternal) != cudaSuccess)

@@ -13,12 +13,17 @@
 // clamped to [0, nPix] (Flat extrapolation).  The forward projector takes the reference's
 // |diff| of F at consecutive detector boundaries from a warp-level prefix scan kept in
 // two-float (hi + lo) arithmetic, so nearby prefix values subtract without losing FP32
-// accuracy; the back-projector evaluates each pixel's |diff| as a local sum over the few
-// detector bins it covers plus the two fractional end terms.  Both are exactly the
-// reference's quantity.  FP64 is kept for the per-view and per-row geometry (trig,
-// boundary mapping); the per-sample work is FP32.
+// accuracy.  The back-projector is the transpose: a warp-level two-float scan of each view's
+// detector-bin integrals gives the detector prefix integral at the knots, and each pixel's
+// value is |G(u1) - G(u0)| of that prefix interpolated at the pixel's two mapped boundaries
+// (:196-205).  Both are exactly the reference's quantity.  FP64 is kept for the per-view and
+// per-row geometry (trig, boundary mapping); the per-sample work is FP32.
 //
-// Quirks kept: detector y offset -(DSD-DS0) - dSize/2 (:29), Flat extrapolation,
+// With BddArgs.arc the detector boundaries lie on the arc of radius DSD about the source
+// (SinoFanArc; an extension with no reference counterpart); everything downstream of the
+// mapped boundaries is shared.
+//
+// Quirks kept: detector y offset -(DSD-DS0) - dSize/2 (:29, flat detector), Flat extrapolation,
 // |diff| (the pair is not linear for signed images), the (na, nDet) sinogram layout,
 // and in backproject_bdd the aliasing reconImgTmp === reconImg (:139-140), which adds
 // the first view's row block once more without the y-axis transpose.
@@ -59,11 +64,18 @@ __device__ __forceinline__ ViewInfo view_info(double beta, double DS0) {
     return vi;
 }
 
-// mapped detector boundary k (0..nDet) for one view, :28-29, 49-50, 60-66
+// mapped detector boundary k (0..nDet) for one view, :28-29, 49-50, 60-66.  Arc detector (an
+// extension; the reference pair is flat-only): boundary k on the circle of radius DSD about the
+// source, at angle (k - nDet/2) dSize / DSD from the central ray, before the view rotation.
 __device__ __forceinline__ double det_boundary(const ViewInfo &vi, double beta, int k, int nDet,
-                                               double DSD, double DS0, double dSize) {
+                                               double DSD, double DS0, double dSize, int arc) {
     double detX = (-(nDet / 2.0) + k) * dSize;
     double detY = -(DSD - DS0) - dSize / 2;
+    if (arc) {
+        const double g = (-(nDet / 2.0) + k) * dSize / DSD;
+        detX = DSD * sin(g);
+        detY = DS0 - DSD * cos(g);
+    }
     double sb = sin(beta), cb = cos(beta);
     double rdX = detX * cb - detY * sb, rdY = detX * sb + detY * cb;
     return vi.axis ? map2x(vi.rtx, vi.rty, rdX, rdY) : map2y(vi.rtx, vi.rty, rdX, rdY);
@@ -96,14 +108,16 @@ __device__ __forceinline__ void row_affine(const ViewInfo &vi, int r, int nPix, 
 }
 
 // ------------------------------------------------------------ per-view set-up
-// forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info, ascending knots K
-// (nDet+1), per-bin integrals B (nDet, ascending order: sino * L * |ddetm|, signed as the
-// reference's prefix, :196) and 1/(K[j+1]-K[j]) (reversed when detm descends, :198-202).
+// forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info, the knot table T
+// (nDet+1 float4 per view: x = knot K[j] in ascending order, y = density B[j] / (K[j+1]-K[j])
+// of bin j, 0 for the last knot; z, w = the prefix, filled by bdd_prefix_kernel) and the
+// per-bin integrals B (nDet, ascending order: sino * L * |ddetm|, signed as the reference's
+// prefix, :196; reversed when detm descends, :198-202).
 // One CTA per (view, chunk of kSetupChunk bins): the view's constants once, each FP64 boundary
 // once into shared memory, then the chunk's outputs from those values (the same FP64 calls).
 constexpr int kSetupChunk = kThreads;
 __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo *info, float *detm, float *L,
-                                                             const float *sino, float *kn, float *kb, float *kinv) {
+                                                             const float *sino, float4 *tab, float *kb) {
     __shared__ ViewInfo vis;
     __shared__ int desc_s;
     __shared__ double bnd[kSetupChunk + 1];
@@ -113,8 +127,8 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
     if (threadIdx.x == 0) {
         vis = view_info(beta, G.DS0);
         if (blockIdx.y == 0) info[p] = vis;
-        desc_s = sino ? det_boundary(vis, beta, 0, nDet, G.DSD, G.DS0, G.dSize) >
-                            det_boundary(vis, beta, 1, nDet, G.DSD, G.DS0, G.dSize)
+        desc_s = sino ? det_boundary(vis, beta, 0, nDet, G.DSD, G.DS0, G.dSize, G.arc) >
+                            det_boundary(vis, beta, 1, nDet, G.DSD, G.DS0, G.dSize, G.arc)
                       : 0;
     }
     __syncthreads();
@@ -123,7 +137,7 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
     // boundaries b0 .. b0 + cnt: those of bins n0 .. n1-1 (reversed for a descending back-projection)
     const int b0 = desc ? nDet - n1 : n0;
     for (int i = threadIdx.x; i <= cnt; i += blockDim.x)
-        bnd[i] = det_boundary(vi, beta, b0 + i, nDet, G.DSD, G.DS0, G.dSize);
+        bnd[i] = det_boundary(vi, beta, b0 + i, nDet, G.DSD, G.DS0, G.dSize, G.arc);
     __syncthreads();
     if (!sino) {
         float *dm = detm + (size_t)p * (nDet + 1);
@@ -132,18 +146,22 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
             L[(size_t)p * nDet + n] = (float)det_scale(vi, bnd[n - n0], bnd[n + 1 - n0], G.pSize);
         return;
     }
-    float *K = kn + (size_t)p * (nDet + 1), *B = kb + (size_t)p * nDet, *KI = kinv + (size_t)p * nDet;
-    for (int k = n0 + threadIdx.x; k <= n1; k += blockDim.x) {
-        const int src = desc ? nDet - k : k;
-        K[k] = (float)bnd[src - b0];
-    }
-    for (int j = n0 + threadIdx.x; j < n1; j += blockDim.x) {
-        // ascending bin j covers reference bin n = desc ? nDet-1-j : j
-        const int n = desc ? nDet - 1 - j : j;
-        const double d0 = bnd[n - b0], d1 = bnd[n + 1 - b0];
-        const double w = ((double)sino[p + (size_t)G.na * n] * det_scale(vi, d0, d1, G.pSize)) * (d1 - d0);
-        B[j] = (float)(desc ? -w : w);  // integral over the bin in the ascending direction
-        KI[j] = (float)(1.0 / std::fabs(d1 - d0));
+    float4 *T = tab + (size_t)p * (nDet + 1);
+    float *B = kb + (size_t)p * nDet;
+    // this chunk writes knots n0 .. n1-1 with their bins, and the last chunk also knot nDet
+    for (int j = n0 + threadIdx.x; j < n1 || (j == nDet && n1 == nDet); j += blockDim.x) {
+        // ascending knot j is reference boundary desc ? nDet-j : j; ascending bin j covers
+        // reference bin n = desc ? nDet-1-j : j
+        const int src = desc ? nDet - j : j;
+        float dens = 0.f;
+        if (j < n1) {
+            const int n = desc ? nDet - 1 - j : j;
+            const double d0 = bnd[n - b0], d1 = bnd[n + 1 - b0];
+            const double w = ((double)sino[p + (size_t)G.na * n] * det_scale(vi, d0, d1, G.pSize)) * (d1 - d0);
+            B[j] = (float)(desc ? -w : w);  // integral over the bin in the ascending direction
+            dens = (float)((desc ? -w : w) / std::fabs(d1 - d0));
+        }
+        T[j] = make_float4((float)bnd[src - b0], dens, 0.f, 0.f);
     }
 }
 
@@ -281,25 +299,69 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------------ backward
-// F(u) over the detector: integral of the bin densities up to u (knots K ascending).
-__device__ __forceinline__ int knot_search(const float *K, int nDet, float u) {
+// Detector prefix integral of one view (integrate1D over the bins, :196): a warp-level scan of
+// the ascending bin integrals B in two-float arithmetic, P[0] = 0, P[j+1] = P[j] + B[j], written
+// into the knot table's (z, w) = (hi, lo).  One warp per view.
+__global__ void __launch_bounds__(kThreads) bdd_prefix_kernel(BddArgs G, const float *kb, float4 *tab) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kWarps + warp;
+    if (p >= G.na) return;  // warp-uniform
+    const int nDet = G.nDet;
+    const float *B = kb + (size_t)p * nDet;
+    float4 *T = tab + (size_t)p * (nDet + 1);
+    const unsigned full = 0xffffffffu;
+    const int chunk = (nDet + 31) / 32;
+    const int j_begin = min(nDet, lane * chunk), j_end = min(nDet, j_begin + chunk);
+    float th = 0.f, tl = 0.f;
+    for (int j = j_begin; j < j_end; j++) two_sum_add(th, tl, B[j]);
+    for (int off = 1; off < 32; off <<= 1) {
+        const float oh = __shfl_up_sync(full, th, off), ol = __shfl_up_sync(full, tl, off);
+        if (lane >= off) {
+            two_sum_add(th, tl, oh);
+            tl += ol;
+        }
+    }
+    float sh = __shfl_up_sync(full, th, 1), sl = __shfl_up_sync(full, tl, 1);
+    if (lane == 0) sh = sl = 0.f;
+    for (int j = j_begin; j < j_end; j++) {
+        T[j].z = sh;
+        T[j].w = sl;
+        two_sum_add(sh, sl, B[j]);
+    }
+    if (lane == 31) {
+        T[nDet].z = th;
+        T[nDet].w = tl;
+    }
+}
+
+// G(u) = P[j] + (u - K[j]) * dens[j] for K[j] <= u <= K[j+1]: the detector prefix integral
+// linearly interpolated at u (:198-203), as (hi, lo).
+__device__ __forceinline__ void prefix_at(const float4 *T, int j, float u, float &gh, float &gl) {
+    const float4 t = T[j];
+    gh = t.z;
+    gl = fmaf(u - t.x, t.y, t.w);
+}
+
+// First knot interval of u: the largest j < nDet with K[j] <= u (0 below the first knot).
+__device__ __forceinline__ int knot_search(const float4 *T, int nDet, float u) {
     int lo = 0, hi = nDet;  // K[lo] <= u < K[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (K[mid] <= u) lo = mid; else hi = mid;
+        if (T[mid].x <= u) lo = mid; else hi = mid;
     }
     return lo;
 }
 
+// Per image row and view: pixel c takes |G(u_{c+1}) - G(u_c)| (:205) at its mapped boundaries
+// u_c = r0 + c delta, clamped to the knots (Flat extrapolation, :199-201); the two-float prefix
+// keeps that difference accurate to FP32 relative to the pixel's own integral.  Each lane owns
+// a run of consecutive pixels and walks the knots along it, reusing G at the shared boundary.
 __global__ void __launch_bounds__(kThreads)
-    bdd_back_kernel(BddArgs G, const ViewInfo *info, const float *kn, const float *kb, const float *kinv,
-                    float *image, int views_per_cta) {
+    bdd_back_kernel(BddArgs G, const ViewInfo *info, const float4 *tab, float *image, int views_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet;
-    float *K = reinterpret_cast<float *>(smraw);  // nDet+1
-    float *B = K + (nDet + 1);                     // nDet
-    float *KI = B + nDet;                          // nDet
-    float *accX = KI + nDet;                       // kWarps x nPix
+    float4 *T = reinterpret_cast<float4 *>(smraw);                 // nDet+1
+    float *accX = reinterpret_cast<float *>(T + (nDet + 1));       // kWarps x nPix
     float *accY = accX + kWarps * nPix;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * kWarps + warp;
@@ -309,42 +371,35 @@ __global__ void __launch_bounds__(kThreads)
     const int per = (nPix + 31) / 32;  // contiguous pixels per lane
     for (int p = v_begin; p < v_end; p++) {
         __syncthreads();
-        for (int k = threadIdx.x; k <= nDet; k += kThreads) K[k] = kn[(size_t)p * (nDet + 1) + k];
-        for (int j = threadIdx.x; j < nDet; j += kThreads) {
-            B[j] = kb[(size_t)p * nDet + j];
-            KI[j] = kinv[(size_t)p * nDet + j];
-        }
+        for (int k = threadIdx.x; k <= nDet; k += kThreads) T[k] = tab[(size_t)p * (nDet + 1) + k];
         __syncthreads();
         if (r >= nPix) continue;
         const ViewInfo vi = info[p];
         double r0d, deltad;
         row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
         const float r0 = (float)r0d, delta = (float)deltad;
-        const float kfirst = K[0], klast = K[nDet];
-        // lane owns pixels [c_a, c_b); walk the knots forward from the first boundary
+        const float kfirst = T[0].x, klast = T[nDet].x;
         const int c_a = lane * per, c_b = min(nPix, c_a + per);
         if (c_a >= c_b) continue;
-        float u0 = fmaf((float)c_a, delta, r0);
-        int j0 = knot_search(K, nDet, fminf(fmaxf(u0, kfirst), klast));
+        float u = fminf(fmaxf(fmaf((float)c_a, delta, r0), kfirst), klast);
+        int j = knot_search(T, nDet, u);
+        float gh, gl;
+        prefix_at(T, j, u, gh, gl);
+        const bool up = delta > 0.f;  // the boundaries ascend (walk the knots forward) or descend
         for (int c = c_a; c < c_b; c++) {
-            const float u1 = fmaf((float)(c + 1), delta, r0);
-            // integral of the detector density over [u0, u1] (clamped to the knots)
-            const float a = fminf(fmaxf(fminf(u0, u1), kfirst), klast);
-            const float b = fminf(fmaxf(fmaxf(u0, u1), kfirst), klast);
-            int ja = j0;
-            while (ja > 0 && K[ja] > a) ja--;
-            while (ja < nDet - 1 && K[ja + 1] <= a) ja++;
-            int jb = ja;
-            while (jb < nDet - 1 && K[jb + 1] <= b) jb++;
-            float sum = -(a - K[ja]) * KI[ja] * B[ja];
-            for (int j = ja; j < jb; j++) sum += B[j];
-            sum += (b - K[jb]) * KI[jb] * B[jb];
-            const float tmp = fabsf(sum);  // :205
-            if (vi.axis) ax[c] += tmp;       // :210
-            else ay[c] += tmp;               // :212
-            if (p == 0) ax[c] += tmp;        // aliasing of :139-140
-            u0 = u1;
-            j0 = jb;
+            u = fminf(fmaxf(fmaf((float)(c + 1), delta, r0), kfirst), klast);
+            if (up)
+                while (j < nDet - 1 && T[j + 1].x <= u) j++;
+            else
+                while (j > 0 && T[j].x > u) j--;
+            float hh, hl;
+            prefix_at(T, j, u, hh, hl);
+            const float tmp = fabsf((hh - gh) + (hl - gl));  // :205
+            if (vi.axis) ax[c] += tmp;                        // :210
+            else ay[c] += tmp;                                // :212
+            if (p == 0) ax[c] += tmp;                         // aliasing of :139-140
+            gh = hh;
+            gl = hl;
         }
     }
     __syncwarp();
@@ -362,7 +417,7 @@ size_t project_smem(const BddArgs &G) {
            sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * G.nDet);
 }
 size_t back_smem(const BddArgs &G) {
-    return sizeof(float) * ((size_t)(G.nDet + 1) + 2 * (size_t)G.nDet + 2 * (size_t)kWarps * G.nPix);
+    return sizeof(float4) * (size_t)(G.nDet + 1) + sizeof(float) * 2 * (size_t)kWarps * G.nPix;
 }
 
 }  // namespace
@@ -372,7 +427,7 @@ size_t bdd_project_scratch(const BddArgs &G) {
 }
 
 size_t bdd_back_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + 2 * (size_t)G.na * G.nDet);
+    return info_bytes(G.na) + sizeof(float4) * (size_t)G.na * (G.nDet + 1) + sizeof(float) * (size_t)G.na * G.nDet;
 }
 
 int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
@@ -384,7 +439,7 @@ int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
     float *detm = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
     float *L = detm + (size_t)G.na * (G.nDet + 1);
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L, nullptr,
-                                                                                             nullptr, nullptr, nullptr);
+                                                                                             nullptr, nullptr);
     return after_launch("bdd_setup_kernel");
 }
 
@@ -423,13 +478,14 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
         return SGB_ERR_ARG;
     }
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
-    float *kn = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
-    float *kb = kn + (size_t)G.na * (G.nDet + 1);
-    float *kinv = kb + (size_t)G.na * G.nDet;
+    float4 *tab = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na));
+    float *kb = reinterpret_cast<float *>(tab + (size_t)G.na * (G.nDet + 1));
     SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, nullptr, nullptr,
-                                                                                             sino, kn, kb, kinv);
+                                                                                             sino, tab, kb);
     SGB_TRY(after_launch("bdd_setup_kernel"));
+    bdd_prefix_kernel<<<(G.na + kWarps - 1) / kWarps, kThreads, 0, st>>>(G, kb, tab);
+    SGB_TRY(after_launch("bdd_prefix_kernel"));
     int gx = (G.nPix + kWarps - 1) / kWarps;
     // views split over CTAs so that each SM holds ~8 of them (row blocks x view groups)
     const int target = 8 * std::max(1, num_sms());
@@ -437,7 +493,7 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
     int vpc = (G.na + vsplit - 1) / vsplit;
     vsplit = (G.na + vpc - 1) / vpc;
     SGB_CUDA(cudaFuncSetAttribute(bdd_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, kn, kb, kinv, image, vpc);
+    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, tab, image, vpc);
     return after_launch("bdd_back_kernel");
 }
 

@@ -54,6 +54,12 @@ size_t filter_scratch_bytes(const FilterOperator &F, long long nrows);
 int launch_filter_rows(const FilterArgs &A, const FilterOperator &F, DevBuf &scratch, void *out, int out_kind,
                        cudaStream_t st);
 
+// F16 storage form of FDK: FP32 filtered rows y (nrows = nt * na rows of `pitch` samples, ns of
+// data) -> FP16 quads (8 bytes per sample, same layout), scaled by a power of two from max|y|;
+// *unscale receives the inverse scale (device word).  `amax` is a device word of scratch.
+int launch_quad_pack(const float *y, int pitch, int ns, int nt, long long nrows, void *quads, unsigned *amax,
+                     float *unscale, cudaStream_t st);
+
 // cuTensorMapEncodeTiled from the driver entry-point table (null when unavailable)
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn();
 
@@ -100,6 +106,7 @@ struct BddArgs {
     int nPix, nDet, na;
     const double *angle;   // device, na
     double DSD, DS0, pSize, dSize;
+    int arc;               // 1: detector boundaries on the arc of radius DSD about the source
 };
 // scratch sizes are returned by the *_scratch functions (bytes).
 size_t bdd_project_scratch(const BddArgs &G);

@@ -12,10 +12,10 @@ _PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(_PKG, "libsinogb300.so")
 
 SGB_OK, SGB_ERR_ARG, SGB_ERR_CUDA, SGB_ERR_NOMEM, SGB_ERR_GEOM, SGB_ERR_UNSUPPORTED, SGB_ERR_TIMEOUT = range(7)
-SGB_DEVICE_PTRS, SGB_ASYNC = 1, 2
+SGB_DEVICE_PTRS, SGB_ASYNC, SGB_BDD_ARC = 1, 2, 4
 SGB_PAR, SGB_ARC, SGB_FLAT = 0, 1, 2
 SGB_WIN = {"none": 0, "boxcar": 1, "hamming": 2, "hann": 3, "vect": 4}
-SGB_STORE_F32, SGB_STORE_BF16 = 0, 1
+SGB_STORE_F32, SGB_STORE_BF16, SGB_STORE_F16 = 0, 1, 2
 SGB_SRC_CIRCLE, SGB_SRC_HELIX = 0, 1
 
 c_int, c_ll, c_double, c_float, c_void_p = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_float, ctypes.c_void_p
@@ -51,6 +51,7 @@ _SIGS = {
     "sgb_version": (c_int, []),
     "sgb_last_error": (c_int, [ctypes.c_char_p, ctypes.c_size_t]),
     "sgb_launch_count": (c_ll, []),
+    "sgb_device_alloc_count": (c_ll, []),
     "sgb_fbp_ramp": (c_int, [c_int, c_int, c_double, c_double, P]),
     "sgb_fbp_window": (c_int, [c_int, c_double, c_int, P, P]),
     "sgb_fbp_filter": (c_int, [c_int, c_int, c_double, c_double, c_int, c_double, P, c_int, P]),
@@ -78,6 +79,8 @@ _SIGS = {
     "sgb_bdd_backproject": (c_int, [P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P, c_int,
                                     P]),
     "sgb_bdd_plan_create": (c_int, [c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, P]),
+    "sgb_bdd_plan_create_det": (c_int, [c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, c_int,
+                                        P]),
     "sgb_bdd_plan_project": (c_int, [P, P, P, c_int, P]),
     "sgb_bdd_plan_backproject": (c_int, [P, P, P, c_int, P]),
     "sgb_bdd_plan_destroy": (c_int, [P]),
@@ -156,6 +159,11 @@ def check(status: int, what: str = "") -> None:
 
 def launch_count() -> int:
     return int(lib().sgb_launch_count())
+
+
+def device_alloc_count() -> int:
+    """Device allocations (cudaMalloc) the library has made since it was loaded."""
+    return int(lib().sgb_device_alloc_count())
 
 
 def measure_peaks(stream=None) -> dict:

@@ -4,6 +4,10 @@
 Layouts follow the reference: the phantom is Julia (nPix, nPix) with row = y (row 1 at
 the top) and col = x, i.e. numpy ``phantom_np[col, row]``; the sinogram is Julia
 (na, nDet), i.e. numpy ``(nDet, na)``.
+
+Extension: ``BddGeo.arc = True`` (or an ``arc`` key in a dict geo) puts the detector boundaries
+on the arc of radius DSD about the source, for SinoFanArc scans; the reference's pair is
+flat-only (bdd_2d.jl:28-29).
 """
 from __future__ import annotations
 
@@ -27,14 +31,18 @@ class BddGeo:
     nPix: int
     nDet: int
     angle: np.ndarray
+    arc: bool = False
 
     @classmethod
     def from_geoms(cls, rg, ig):
-        """geo tuple as built in test/sys2/bdd_2d.jl:45-46 from SinoFanFlat + ImageGeom."""
-        return cls(rg.dsd, _dso(rg), ig.deltas[0], rg.d, ig.dims[0], rg.nb, _ar(rg))
+        """geo tuple as built in test/sys2/bdd_2d.jl:21-22 from a fan-beam SinoGeom + ImageGeom;
+        a SinoFanArc gives the arc-detector pair."""
+        return cls(rg.dsd, _dso(rg), ig.deltas[0], rg.d, ig.dims[0], rg.nb, _ar(rg), bool(getattr(rg, "kind", "") == "arc"))
 
 
 def _g(geo, k):
+    if k == "arc":
+        return bool(geo.get("arc", False)) if isinstance(geo, dict) else bool(getattr(geo, "arc", False))
     return geo[k] if isinstance(geo, dict) else getattr(geo, k)
 
 
@@ -42,9 +50,10 @@ def _run(fn, x, geo, out_shape):
     a = Arr(x)
     ang = f64(_g(geo, "angle"))
     out = empty(out_shape, a)
+    flags = flags_for(a.device) | (_lib.SGB_BDD_ARC if _g(geo, "arc") else 0)
     st = getattr(_lib.lib(), fn)(a.ptr, int(_g(geo, "nPix")), int(_g(geo, "nDet")), len(ang), ptr(ang),
                                  float(_g(geo, "DSD")), float(_g(geo, "DS0")), float(_g(geo, "pSize")),
-                                 float(_g(geo, "dSize")), ptr(out), flags_for(a.device), stream_for(a.device))
+                                 float(_g(geo, "dSize")), ptr(out), flags, stream_for(a.device))
     if st == _lib.SGB_ERR_ARG:
         raise SinogramsArgumentError(_lib.last_error())
     _lib.check(st, fn)
@@ -78,9 +87,10 @@ class BddPlan:
         ang = f64(_g(geo, "angle"))
         self.na = len(ang)
         self._h = ctypes.c_void_p()
-        st = _lib.lib().sgb_bdd_plan_create(self.nPix, self.nDet, self.na, ptr(ang), float(_g(geo, "DSD")),
-                                            float(_g(geo, "DS0")), float(_g(geo, "pSize")),
-                                            float(_g(geo, "dSize")), ctypes.byref(self._h))
+        det = _lib.SGB_ARC if _g(geo, "arc") else _lib.SGB_FLAT
+        st = _lib.lib().sgb_bdd_plan_create_det(self.nPix, self.nDet, self.na, ptr(ang), float(_g(geo, "DSD")),
+                                                float(_g(geo, "DS0")), float(_g(geo, "pSize")),
+                                                float(_g(geo, "dSize")), det, ctypes.byref(self._h))
         if st == _lib.SGB_ERR_ARG:
             raise SinogramsArgumentError(_lib.last_error())
         _lib.check(st, "bdd_plan_create")
