@@ -11,8 +11,9 @@ ramp-filtered rows onto the ramp-filtered rows of the noise-free data.
 
 The training data are generated here, on the GPU, by the method itself: random-ellipse
 phantoms rasterised onto the image grid and projected by the distance-driven projector
-(project_bdd, src/sys2/bdd_2d.jl), with Gaussian noise.  The reference's projector is
-flat-detector only (bdd_2d.jl:28-29), so this pipeline uses a SinoFanFlat geometry.
+(project_bdd, src/sys2/bdd_2d.jl), with Gaussian noise.  The workload's geometry is SinoFanArc;
+the reference's projector is flat-detector only (bdd_2d.jl:28-29), so data generation and the
+judge use this library's arc-detector form of the pair (BddGeo.arc).
 
 `fbp_learned(..., judge=True)` keeps the learned image only when its reprojection
 residual through the same projector does not exceed the plain ramp FBP's by more than
@@ -30,7 +31,7 @@ from . import _lib
 from ._arrays import Arr, f64, flags_for, ptr, stream_for
 from .bdd import BddGeo, BddPlan
 from .filters import SinogramsArgumentError
-from .geom import ImageGeom, SinoFanFlat, _rfov
+from .geom import ImageGeom, SinoFanArc, SinoFanFlat, _rfov
 from .phantoms import random_ellipses
 from .recon import FBPNormalPlan, _status, fbp, plan_fbp
 
@@ -42,11 +43,14 @@ except Exception:  # pragma: no cover
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "weights")
 
 
-def sparse_fan_geometry(na: int = 90):
+def sparse_fan_geometry(na: int = 90, detector: str = "arc"):
     """The sparse-view fan-beam geometry of the learned-filter workload: nb = 888, d = 1.0239,
     dsd = 949.075, dod = 408.075 (the GE LightSpeed values of type2.jl:381-402), na views over
-    360 degrees, flat detector; 512 x 512 image at 0.9766 mm with the FOV disk as mask."""
-    rg = SinoFanFlat(nb=888, d=1.0239, na=na, orbit=360.0, dsd=949.075, dod=408.075)
+    360 degrees, an arc detector (SinoFanArc; detector="flat" gives SinoFanFlat); 512 x 512 image
+    at 0.9766 mm with the FOV disk as mask.  The distance-driven projector that generates the
+    training data and judges the result uses the same detector."""
+    cls = {"arc": SinoFanArc, "flat": SinoFanFlat}[detector]
+    rg = cls(nb=888, d=1.0239, na=na, orbit=360.0, dsd=949.075, dod=408.075)
     ig = ImageGeom((512, 512), (0.9766, 0.9766))
     return rg, ig.with_mask(ig.circle(_rfov(rg)))
 
@@ -199,7 +203,7 @@ def ellipse_image(ig: ImageGeom, ell, sub: int = 2, device: bool = True):
 
 def image_to_dd(img):
     """ImageGeom-order image (ny, nx) -> project_bdd phantom layout (Julia (nPix,nPix), row 1
-    = top = largest y), as test/sys2/bdd_2d.jl:155 does with reverse(rot180(img'), dims=2)."""
+    = top = largest y), as test/sys2/bdd_2d.jl:31 does with reverse(rot180(img'), dims=2)."""
     return torch.flip(img, dims=[0]).T.contiguous()
 
 
@@ -211,7 +215,7 @@ def bdd_plan(geo: BddGeo) -> BddPlan:
     many images through one geometry)."""
     ang = f64(geo.angle)
     key = (float(geo.DSD), float(geo.DS0), float(geo.pSize), float(geo.dSize), int(geo.nPix), int(geo.nDet),
-           ang.tobytes())
+           ang.tobytes(), bool(getattr(geo, "arc", False)))
     plan = _BDD_PLANS.get(key)
     if plan is None:
         if len(_BDD_PLANS) >= 8:
@@ -398,9 +402,9 @@ def fbp_learned_ramp(plan_learned: FBPNormalPlan, plan_plain: FBPNormalPlan, sin
     return (img_l if used == "learned" else img_p), {"used": used, "residual_learned": rl, "residual_plain": rp}
 
 
-def default_ramp_path() -> str:
-    return os.path.join(WEIGHTS_DIR, "learned_ramp_fanflat888_90v.npz")
+def default_ramp_path(detector: str = "arc") -> str:
+    return os.path.join(WEIGHTS_DIR, f"learned_ramp_fan{detector}888_90v.npz")
 
 
-def default_weights_path() -> str:
-    return os.path.join(WEIGHTS_DIR, "learned_filter_fanflat888_90v.npz")
+def default_weights_path(detector: str = "arc") -> str:
+    return os.path.join(WEIGHTS_DIR, f"learned_filter_fan{detector}888_90v.npz")

@@ -12,7 +12,8 @@ least-squares per-frequency gain) and compares it with plain FBP at the same lat
 
 Data: seeded random-ellipse phantoms (20 ellipses, centres r <= 220 mm, semi-axes
 U[4,120] mm, density U[-0.3,1]) rasterised on the 512^2 grid, projected by the
-distance-driven projector over 90 views of the sparse fan geometry, plus Gaussian noise
+distance-driven projector over 90 views of the sparse fan geometry (arc detector unless
+--detector flat), plus Gaussian noise
 (sigma = 0.5% of each sinogram's peak).  Target: the plan's ramp-filtered rows of the
 noise-free sinogram.  Prints one JSON summary line.
 """
@@ -115,10 +116,14 @@ def main():
     ap.add_argument("--checkpoint", help="save params, scale and Adam state here when the run stops")
     ap.add_argument("--stop", type=int, help="stop after this many steps of the schedule (with --checkpoint)")
     ap.add_argument("--resume", help="continue the schedule from a checkpoint (same data arguments)")
+    ap.add_argument("--detector", default="arc", choices=["arc", "flat"],
+                    help="SinoFanArc (the workload's geometry) or SinoFanFlat")
     args = ap.parse_args()
-    rg, ig = LF.sparse_fan_geometry()
+    rg, ig = LF.sparse_fan_geometry(detector=args.detector)
+    if args.out == LF.default_weights_path():
+        args.out = LF.default_weights_path(args.detector)
     if args.linear:
-        out = args.out if args.out != LF.default_weights_path() else LF.default_ramp_path()
+        out = args.out if args.out != LF.default_weights_path(args.detector) else LF.default_ramp_path(args.detector)
         if args.eval_only:
             lr = LF.LearnedRamp.load(out)
         else:

@@ -145,3 +145,29 @@ def test_committed_learned_ramp_beats_plain_fbp(cuda):
         rm_p.append(float(((S.fbp(plain, s) - img)[mask]).pow(2).mean().sqrt()))
         rm_l.append(float(((S.fbp(learned, s) - img)[mask]).pow(2).mean().sqrt()))
     assert np.mean(rm_l) < np.mean(rm_p), (rm_l, rm_p)
+
+
+def test_judge_falls_back_to_plain_fbp(cuda):
+    """When the learned image reprojects worse than plain ramp FBP, the judge returns the plain
+    image, bit for bit the image fbp(plan, sino) gives: a CNN with a deliberately wrong last
+    layer (large random weights) and a learned ramp with a wrong gain (x5 above the band centre)."""
+    import torch
+    rg, ig = LF.sparse_fan_geometry()
+    plan = S.plan_fbp(rg, ig)
+    geo = S.BddGeo.from_geoms(rg, ig)
+    img = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(920000))
+    s = LF.dd_project(img, geo)
+    s = s + 0.005 * s.abs().max() * torch.randn(s.shape, device="cuda",
+                                               generator=torch.Generator(device="cuda").manual_seed(7))
+    plain = S.fbp(plan, s)
+    rng = np.random.default_rng(5)
+    bad = LF.LearnedFilter(scale=float(s.abs().max()), params=(0.5 * rng.standard_normal(LF.NPARAM)).astype(np.float32))
+    out, info = LF.fbp_learned(plan, bad, s, judge=True)
+    assert info["used"] == "plain" and info["residual_learned"] > info["residual_plain"], info
+    assert torch.equal(out, plain)
+    npad = len(plan.filter)
+    k = np.minimum(np.arange(npad), npad - np.arange(npad))
+    wrong = LF.LearnedRamp(np.where(k > npad // 8, 5.0, 1.0), npad)
+    out2, info2 = LF.fbp_learned_ramp(wrong.plan(rg, ig), plan, s, judge=True)
+    assert info2["used"] == "plain", info2
+    assert torch.equal(out2, plain)

@@ -73,11 +73,11 @@ def test_ramp_and_window():
 
 def test_errors_like_reference():
     with pytest.raises(S.SinogramsArgumentError, match="N must be even"):
-        S.ramp_flat(7, 1.0)  # ramp.jl:234
+        S.ramp_flat(7, 1.0)  # ramp.jl:87
     with pytest.raises(S.SinogramsArgumentError, match="physically impossible"):
-        S.ramp_arc(4096, 1.0, 100.0)  # ramp.jl:217-219
+        S.ramp_arc(4096, 1.0, 100.0)  # ramp.jl:70-72
     with pytest.raises(S.SinogramsArgumentError, match="N mismatch"):
-        S.fbp_window(S.Window(np.ones(7)), 8)  # window.jl:310
+        S.fbp_window(S.Window(np.ones(7)), 8)  # window.jl:72
     with pytest.raises(S.SinogramsArgumentError, match="Parker"):
         S.parker_weight(S.SinoPar(orbit=361))  # parker.jl:45
     with pytest.raises(S.SinogramsArgumentError, match="Unequal"):
@@ -178,11 +178,12 @@ def test_footprint_size_bad_dso():
         O.footprint_size(g, dict(dims=(80, 80, 4), deltas=(1.0, 1.0, 1.0)))
 
 
-def test_learned_ramp_gain_file_and_round_trip(tmp_path):
+@pytest.mark.parametrize("detector", ["arc", "flat"])
+def test_learned_ramp_gain_file_and_round_trip(tmp_path, detector):
     """The committed learned-ramp gain is even (a real, symmetric row filter), passes DC and
     only attenuates; a saved gain loads back unchanged; a gain of the wrong length is refused."""
     from sinograms import learned as LF
-    lr = LF.LearnedRamp.load(LF.default_ramp_path())
+    lr = LF.LearnedRamp.load(LF.default_ramp_path(detector))
     g = lr.gain
     assert g.shape == (lr.npad,) and np.array_equal(g[1:], g[1:][::-1])
     assert abs(g[0] - 1.0) < 1e-3 and g.max() < 1.01 and g.min() > 0.0
