@@ -299,6 +299,11 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------------ backward
+// words per warp of the back-projector's skewed pixel accumulators (pixel c at c + c / 16)
+__host__ __device__ __forceinline__ int back_acc_pitch(int nPix) { return nPix + nPix / 16 + 1; }
+// float4 slots of the swizzled knot table: nDet + 1 knots rounded up to whole groups of 8
+__host__ __device__ __forceinline__ int back_tab_slots(int nDet) { return (nDet + 1 + 7) / 8 * 8; }
+
 // Detector prefix integral of one view (integrate1D over the bins, :196): a warp-level scan of
 // the ascending bin integrals B in two-float arithmetic, P[0] = 0, P[j+1] = P[j] + B[j], written
 // into the knot table's (z, w) = (hi, lo).  One warp per view.
@@ -334,10 +339,14 @@ __global__ void __launch_bounds__(kThreads) bdd_prefix_kernel(BddArgs G, const f
     }
 }
 
+// Shared-memory slot of knot j: XOR-swizzled within groups of 8 float4 (the 32 banks), so lanes
+// whose knots lie a fixed stride apart (each walks its own run of pixels) spread over the banks.
+__device__ __forceinline__ int tix(int j) { return j ^ ((j >> 3) & 7); }
+
 // G(u) = P[j] + (u - K[j]) * dens[j] for K[j] <= u <= K[j+1]: the detector prefix integral
 // linearly interpolated at u (:198-203), as (hi, lo).
 __device__ __forceinline__ void prefix_at(const float4 *T, int j, float u, float &gh, float &gl) {
-    const float4 t = T[j];
+    const float4 t = T[tix(j)];
     gh = t.z;
     gl = fmaf(u - t.x, t.y, t.w);
 }
@@ -347,7 +356,7 @@ __device__ __forceinline__ int knot_search(const float4 *T, int nDet, float u) {
     int lo = 0, hi = nDet;  // K[lo] <= u < K[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (T[mid].x <= u) lo = mid; else hi = mid;
+        if (T[tix(mid)].x <= u) lo = mid; else hi = mid;
     }
     return lo;
 }
@@ -360,25 +369,28 @@ __global__ void __launch_bounds__(kThreads)
     bdd_back_kernel(BddArgs G, const ViewInfo *info, const float4 *tab, float *image, int views_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet;
-    float4 *T = reinterpret_cast<float4 *>(smraw);                 // nDet+1
-    float *accX = reinterpret_cast<float *>(T + (nDet + 1));       // kWarps x nPix
-    float *accY = accX + kWarps * nPix;
+    // per-warp pixel accumulators, skewed by one word per 16 pixels: a lane's run of pixels starts
+    // 16 pixels after its neighbour's, so the skew spreads the lanes over the banks
+    const int apitch = back_acc_pitch(nPix);
+    float4 *T = reinterpret_cast<float4 *>(smraw);                      // nDet+1 knots in tix order
+    float *accX = reinterpret_cast<float *>(T + back_tab_slots(nDet));  // kWarps x apitch
+    float *accY = accX + kWarps * apitch;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * kWarps + warp;
-    for (int i = threadIdx.x; i < 2 * kWarps * nPix; i += kThreads) accX[i] = 0.f;
-    float *ax = accX + warp * nPix, *ay = accY + warp * nPix;
+    for (int i = threadIdx.x; i < 2 * kWarps * apitch; i += kThreads) accX[i] = 0.f;
+    float *ax = accX + warp * apitch, *ay = accY + warp * apitch;
     const int v_begin = blockIdx.y * views_per_cta, v_end = min(G.na, v_begin + views_per_cta);
     const int per = (nPix + 31) / 32;  // contiguous pixels per lane
     for (int p = v_begin; p < v_end; p++) {
         __syncthreads();
-        for (int k = threadIdx.x; k <= nDet; k += kThreads) T[k] = tab[(size_t)p * (nDet + 1) + k];
+        for (int k = threadIdx.x; k <= nDet; k += kThreads) T[tix(k)] = tab[(size_t)p * (nDet + 1) + k];
         __syncthreads();
         if (r >= nPix) continue;
         const ViewInfo vi = info[p];
         double r0d, deltad;
         row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
         const float r0 = (float)r0d, delta = (float)deltad;
-        const float kfirst = T[0].x, klast = T[nDet].x;
+        const float kfirst = T[tix(0)].x, klast = T[tix(nDet)].x;
         const int c_a = lane * per, c_b = min(nPix, c_a + per);
         if (c_a >= c_b) continue;
         float u = fminf(fmaxf(fmaf((float)c_a, delta, r0), kfirst), klast);
@@ -389,15 +401,16 @@ __global__ void __launch_bounds__(kThreads)
         for (int c = c_a; c < c_b; c++) {
             u = fminf(fmaxf(fmaf((float)(c + 1), delta, r0), kfirst), klast);
             if (up)
-                while (j < nDet - 1 && T[j + 1].x <= u) j++;
+                while (j < nDet - 1 && T[tix(j + 1)].x <= u) j++;
             else
-                while (j > 0 && T[j].x > u) j--;
+                while (j > 0 && T[tix(j)].x > u) j--;
             float hh, hl;
             prefix_at(T, j, u, hh, hl);
             const float tmp = fabsf((hh - gh) + (hl - gl));  // :205
-            if (vi.axis) ax[c] += tmp;                        // :210
-            else ay[c] += tmp;                                // :212
-            if (p == 0) ax[c] += tmp;                         // aliasing of :139-140
+            const int ca = c + (c >> 4);
+            if (vi.axis) ax[ca] += tmp;                       // :210
+            else ay[ca] += tmp;                               // :212
+            if (p == 0) ax[ca] += tmp;                        // aliasing of :139-140
             gh = hh;
             gl = hl;
         }
@@ -405,8 +418,9 @@ __global__ void __launch_bounds__(kThreads)
     __syncwarp();
     if (r >= nPix) return;
     for (int c = lane; c < nPix; c += 32) {
-        if (ax[c] != 0.f) atomicAdd(image + r + (size_t)nPix * c, ax[c]);
-        if (ay[c] != 0.f) atomicAdd(image + (nPix - 1 - c) + (size_t)nPix * r, ay[c]);  // reverse(., 2)'
+        const float vx = ax[c + (c >> 4)], vy = ay[c + (c >> 4)];
+        if (vx != 0.f) atomicAdd(image + r + (size_t)nPix * c, vx);
+        if (vy != 0.f) atomicAdd(image + (nPix - 1 - c) + (size_t)nPix * r, vy);  // reverse(., 2)'
     }
 }
 
@@ -417,7 +431,7 @@ size_t project_smem(const BddArgs &G) {
            sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * G.nDet);
 }
 size_t back_smem(const BddArgs &G) {
-    return sizeof(float4) * (size_t)(G.nDet + 1) + sizeof(float) * 2 * (size_t)kWarps * G.nPix;
+    return sizeof(float4) * (size_t)back_tab_slots(G.nDet) + sizeof(float) * 2 * (size_t)kWarps * back_acc_pitch(G.nPix);
 }
 
 }  // namespace
