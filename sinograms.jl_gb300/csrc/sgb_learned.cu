@@ -7,9 +7,11 @@
 // filter is exactly the plain ramp.
 //
 // Training kernels (hand-written; BF16 weights, FP32 activations and accumulation):
-//   conv_fwd      y[r,co,t] = b[co] + sum_{ci,k} W[co,ci,k] x[r,ci,t+k-4]  (+ GELU)
+//   conv32_tc     the 32 -> 32 layers' forward (+ bias, GELU) and data gradient (transposed,
+//                 flipped weights) on the tcgen05 tensor cores (see the comment above it)
+//   conv_fwd      y[r,co,t] = b[co] + sum_{ci,k} W[co,ci,k] x[r,ci,t+k-4]  (+ GELU), SIMT, for
+//                 the 1 -> 32 layer and the last layer's data gradient
 //   conv_fwd_c1   the same for one output channel
-//   (data gradient = conv_fwd with the transposed, flipped weights)
 //   conv_wgrad    dW[co,ci,k] = sum_{r,t} g[r,co,t] x[r,ci,t+k-4], db[co] = sum g
 //   gelu_bwd, loss (MSE on the residual), adam
 // Activations are (rows, channels, L) with L = detector samples, zero padded by 4.
@@ -468,6 +470,139 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
 }
 
 
+// ------------------------------------------------------- training on tcgen05
+// The training passes' 32 -> 32 convolutions (the forward of layers 1-3 and the data gradient
+// through them) as implicit GEMMs on the tensor cores, one tile of 128 positions of one row at
+// a time: D[t, co] = sum_{k, ci} X[ci, t + k - 4] Wk[co, ci], M = 128 positions (TMEM lanes),
+// N = 32 channels, K = 9 taps x 32 channels, in the operand layout of lf_tc_fused (the
+// canonical no-swizzle K-major layout; tap k is the staged tile advanced by k positions).
+// Activations and gradients stay FP32 and channel-major in global memory, (rows, 32, L), as
+// the SIMT passes keep them; each staged value is split into three BF16 pieces (hi, mid, lo:
+// 24 significant bits, the FP32 value) and the weights are the network's BF16 weights, so the
+// products are exact and D accumulates them in FP32.  The epilogue adds the bias and writes
+// the pre-activation and GELU(pre) (forward) or the plain sum (data gradient).
+constexpr int kTrPieces = 3;
+constexpr int kTrThreads = 128;  // 4 warps: warp w owns TMEM lanes 32w .. 32w+31 (positions)
+constexpr int kTrABytes = kTrPieces * (kC / 8) * kTPos * 16;
+constexpr size_t kTrSmem = (size_t)kTcWBytes + kTrABytes + sizeof(float) * kC + 64;
+
+template <bool ACT, bool BIAS>
+__global__ void __launch_bounds__(kTrThreads) conv32_tc(const float *__restrict__ in,
+                                                      const __nv_bfloat16 *__restrict__ wp,
+                                                      const float *__restrict__ b, float *__restrict__ pre,
+                                                      float *__restrict__ out, int L, long long R, int *err) {
+    extern __shared__ __align__(128) uint8_t tsm[];
+    uint8_t *Wl = tsm;                                     // [tap][ci / 8][co][8] BF16
+    uint8_t *A = Wl + kTcWBytes;                           // [piece][ci / 8][position][8] BF16
+    float *bias = reinterpret_cast<float *>(A + kTrABytes);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(((uintptr_t)(bias + kC) + 7) & ~uintptr_t(7));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int i = tid; i < kTcWBytes / 16; i += kTrThreads)
+        reinterpret_cast<uint4 *>(Wl)[i] = reinterpret_cast<const uint4 *>(wp)[i];
+    if (tid < kC) bias[tid] = BIAS ? b[tid] : 0.f;
+    if (tid == 0) {
+        dev::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 32);
+        tc::tmem_relinquish();
+    }
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *slot;
+    const uint32_t a_s = dev::smem_u32(A), w_s = dev::smem_u32(Wl);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(kTM, kC);
+    const int tpr = (L + kTM - 1) / kTM;
+    const long long ntiles = R * tpr;
+    uint32_t phase = 0;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long r = tile / tpr;
+        const int t0 = (int)(tile % tpr) * kTM;
+        const float *x = in + r * kC * (long long)L;
+        // stage positions p = 0 .. 135 (t = t0 - 4 + p) of the 32 channels: one item is one
+        // position and one group of 8 channels; consecutive threads take consecutive positions
+        for (int idx = tid; idx < kTPos * (kC / 8); idx += kTrThreads) {
+            const int pp = idx % kTPos, cg = idx / kTPos;
+            const int t = t0 - kPad + pp;
+            const bool in_row = t >= 0 && t < L;
+            uint32_t h[kTrPieces][4];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                float a0 = in_row ? __ldg(x + (long long)(cg * 8 + 2 * j) * L + t) : 0.f;
+                float a1 = in_row ? __ldg(x + (long long)(cg * 8 + 2 * j + 1) * L + t) : 0.f;
+#pragma unroll
+                for (int pc = 0; pc < kTrPieces; pc++) {
+                    const __nv_bfloat162 v = __floats2bfloat162_rn(a0, a1);
+                    const float2 vf = __bfloat1622float2(v);
+                    h[pc][j] = *reinterpret_cast<const uint32_t *>(&v);
+                    a0 -= vf.x;
+                    a1 -= vf.y;
+                }
+            }
+#pragma unroll
+            for (int pc = 0; pc < kTrPieces; pc++)
+                *reinterpret_cast<uint4 *>(A + ((pc * (kC / 8) + cg) * kTPos + pp) * 16) =
+                    make_uint4(h[pc][0], h[pc][1], h[pc][2], h[pc][3]);
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        int good = 1;
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint64_t a0 = sdesc_k_none(a_s, kTPos * 16, 128), b0 = sdesc_k_none(w_s, kC * 16, 128);
+            int n = 0;
+#pragma unroll
+            for (int pc = 0; pc < kTrPieces; pc++)
+#pragma unroll
+                for (int k = 0; k < kK; k++)
+#pragma unroll
+                    for (int ks = 0; ks < kC / 16; ks++, n++)
+                        tc::mma_bf16(tbase, a0 + (uint64_t)((pc * (kC / 8) + 2 * ks) * kTPos + k),
+                                     b0 + (uint64_t)((k * (kC / 8) + 2 * ks) * kC), idesc, n != 0);
+            tc::commit(bar);
+            const long long c0 = clock64();
+            while (!dev::mbar_try_wait(bar, phase & 1))
+                if (clock64() - c0 > dev::kWaitBudget) {
+                    atomicOr(err, 1);
+                    good = 0;
+                    break;
+                }
+        }
+        good = __syncthreads_and(good);
+        phase++;
+        tc::fence_after_sync();
+        if (!good) break;
+        {
+            float v[32];
+            tc::ld32(tbase + ((uint32_t)(32 * warp) << 16), v);
+            const int t = t0 + 32 * warp + lane;
+            if (t < L) {
+                float *o = out + r * kC * (long long)L + t;
+                float *q = ACT ? pre + r * kC * (long long)L + t : nullptr;
+#pragma unroll
+                for (int co = 0; co < kC; co++) {
+                    const float a = v[co] + bias[co];
+                    if (ACT) {
+                        q[(long long)co * L] = a;
+                        o[(long long)co * L] = gelu(a);
+                    } else {
+                        o[(long long)co * L] = a;
+                    }
+                }
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();  // TMEM read and staging buffer free before the next tile
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 32);
+}
+
 // Adam on the FP32 master parameters; refreshes the BF16 weights and the transposed,
 // flipped BF16 weights the data-gradient convolution uses.
 struct LayerOffsets {
@@ -522,6 +657,10 @@ struct sgb_lf {
     // tensor-core inference: packed weights of the 32 -> 32 layers (valid for twp_step), error flag
     DevBuf twp, terr;
     long long twp_step = -1;
+    // tensor-core training: packed weights of layers 1-3 and of their transposes (data gradient),
+    // valid for trp_step
+    DevBuf trp;
+    long long trp_step = -1;
 };
 
 namespace {
@@ -553,15 +692,53 @@ int launch_conv(const float *in, const __nv_bfloat16 *W, const float *b, float *
 
 unsigned grid_for(long long n) { return (unsigned)std::min<long long>((n + 255) / 256, 152 * 16); }
 
-// forward through the 5 layers; act[0] must hold z/s; result (net output) in act[5]
+// The training passes' packed tensor-core weights: layers 1-3 (forward) in slots 0-2, their
+// transposed, flipped weights (data gradient) in slots 3-5, repacked after each Adam step.
+int lf_train_weights(sgb_lf *F, cudaStream_t st) {
+    SGB_TRY(F->trp.reserve(sizeof(__nv_bfloat16) * 6 * kK * kC * kC));
+    SGB_TRY(F->terr.reserve(sizeof(int)));
+    SGB_CUDA(cudaMemsetAsync(F->terr.p, 0, sizeof(int), st));
+    if (F->trp_step == F->step) return SGB_OK;
+    __nv_bfloat16 *tp = F->trp.as<__nv_bfloat16>();
+    for (int l = 1; l <= 3; l++) {
+        lf_tc_weights<<<9, 1024, 0, st>>>(F->wb.as<__nv_bfloat16>() + F->wbase[l], tp + (l - 1) * kK * kC * kC);
+        SGB_TRY(after_launch("lf_tc_weights"));
+        lf_tc_weights<<<9, 1024, 0, st>>>(F->wt.as<__nv_bfloat16>() + F->wbase[l], tp + (l + 2) * kK * kC * kC);
+        SGB_TRY(after_launch("lf_tc_weights"));
+    }
+    F->trp_step = F->step;
+    return SGB_OK;
+}
+
+template <bool ACT, bool BIAS>
+int launch_conv32_tc(sgb_lf *F, const float *in, int slot, const float *b, float *pre, float *out, int L, long long R,
+                     cudaStream_t st) {
+    auto k = conv32_tc<ACT, BIAS>;
+    int dev = 0;
+    SGB_CUDA(cudaGetDevice(&dev));
+    static bool attr_done[64] = {};  // per device
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        SGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrSmem));
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
+    const long long ntiles = R * ((L + kTM - 1) / kTM);
+    const unsigned grid = (unsigned)std::min<long long>(ntiles, 4ll * num_sms());
+    k<<<grid, kTrThreads, kTrSmem, st>>>(in, F->trp.as<__nv_bfloat16>() + slot * kK * kC * kC, b, pre, out, L, R,
+                                          F->terr.as<int>());
+    return after_launch("conv32_tc");
+}
+
+// forward through the 5 layers; act[0] must hold z/s; result (net output) in act[5].  Layers 1-3
+// (32 -> 32) on the tensor cores, the 1 -> 32 and 32 -> 1 layers in SIMT.
 int lf_forward(sgb_lf *F, long long R, int L, cudaStream_t st) {
     const __nv_bfloat16 *wb = F->wb.as<__nv_bfloat16>();
     const float *p = F->p.as<float>();
+    SGB_TRY(lf_train_weights(F, st));
     SGB_TRY((launch_conv<1, kC, true, true>(F->act[0].as<float>(), wb + F->wbase[0], p + F->off.b[0],
                                             F->pre[0].as<float>(), F->act[1].as<float>(), L, R, st)));
     for (int l = 1; l < kLayers - 1; l++)
-        SGB_TRY((launch_conv<kC, kC, true, true>(F->act[l].as<float>(), wb + F->wbase[l], p + F->off.b[l],
-                                                 F->pre[l].as<float>(), F->act[l + 1].as<float>(), L, R, st)));
+        SGB_TRY((launch_conv32_tc<true, true>(F, F->act[l].as<float>(), l - 1, p + F->off.b[l], F->pre[l].as<float>(),
+                                              F->act[l + 1].as<float>(), L, R, st)));
     conv_fwd_c1<kC><<<dim3((L + 127) / 128, (unsigned)R), 128, 0, st>>>(
         F->act[kLayers - 1].as<float>(), wb + F->wbase[kLayers - 1], p + F->off.b[kLayers - 1],
         F->act[kLayers].as<float>(), L, true);
@@ -630,7 +807,7 @@ int lf_backward(sgb_lf *F, long long R, int L, cudaStream_t st) {
             conv_wgrad<kC, kC><<<wgrid, 256, 0, st>>>(F->act[l].as<float>(), gcur, g + F->off.w[l], g + F->off.b[l],
                                                        L, R);
             SGB_TRY(after_launch("conv_wgrad"));
-            SGB_TRY((launch_conv<kC, kC, false, false>(gcur, wt + F->wbase[l], nullptr, nullptr, gnext, L, R, st)));
+            SGB_TRY((launch_conv32_tc<false, false>(F, gcur, l + 2, nullptr, nullptr, gnext, L, R, st)));
             std::swap(gcur, gnext);
         }
     }
@@ -649,6 +826,17 @@ int lf_stage_input(sgb_lf *F, const float *z, long long R, int L, int flags, Dev
     *zdev = static_cast<const float *>(d);
     scale_copy<<<grid_for(R * (long long)L), 256, 0, st>>>(*zdev, 1.f / F->scale, F->act[0].as<float>(), R * (long long)L);
     return after_launch("scale_copy");
+}
+
+// After a synchronisation: the tensor-core passes' error flag (a bounded wait that expired).
+int lf_check_tc(sgb_lf *F, const char *what) {
+    int e = 0;
+    SGB_CUDA(cudaMemcpy(&e, F->terr.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        set_error("%s: tensor-core convolution reported a wait timeout", what);
+        return SGB_ERR_TIMEOUT;
+    }
+    return SGB_OK;
 }
 
 }  // namespace
@@ -766,7 +954,7 @@ int sgb_lf_loss_grad(sgb_lf *F, const float *z, const float *target, long long r
     }
     SGB_CUDA(cudaMemcpyAsync(loss, F->loss.p, sizeof(double), cudaMemcpyDeviceToHost, st));
     SGB_CUDA(cudaStreamSynchronize(st));
-    return SGB_OK;
+    return lf_check_tc(F, "lf_loss_grad");
 }
 
 // one Adam step on a batch of rows (z: ramp-filtered noisy rows, target: ramp-filtered clean rows)
@@ -801,8 +989,10 @@ int sgb_lf_train_step(sgb_lf *F, const float *z, const float *target, long long 
         SGB_CUDA(cudaStreamSynchronize(st));
     } else if (!(flags & SGB_ASYNC)) {
         SGB_CUDA(cudaStreamSynchronize(st));
+    } else {
+        return SGB_OK;
     }
-    return SGB_OK;
+    return lf_check_tc(F, "lf_train_step");
 }
 
 // Adam state for checkpoint and resume.  Both calls first wait for all work on the device, so
