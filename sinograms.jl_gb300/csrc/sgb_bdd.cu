@@ -298,6 +298,143 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// The same projection with the bins, not the rows, split over the warps: each warp scans the
+// prefix of one of the CTA's kWarps staged rows, then walks its own range of at most NG
+// 32-bin groups across all kWarps rows, so its bin sums stay in registers.  Shared memory is
+// the staged rows and their prefixes only (no per-warp bin accumulators), which lets four CTAs
+// share an SM instead of two.  Each warp evaluates F once more per row than its groups (the
+// boundary past its last bin), and the rows of a bin are summed in ascending order.
+struct RowMap {
+    float r0, rdelta, adelta, pad;
+};
+static_assert(kWarps % 4 == 0, "the row maps follow the staged rows at a 16-byte boundary");
+
+template <int NG>
+__global__ void __launch_bounds__(kThreads, 4)
+    bdd_project_bins_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L,
+                            const float *__restrict__ phantom, float *sino, int rows_per_cta) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    const int nPix = G.nPix, nDet = G.nDet, p = blockIdx.x;
+    float2 *pw = reinterpret_cast<float2 *>(smraw);                   // kWarps x (nPix+1): prefix (hi, lo)
+    float *vw = reinterpret_cast<float *>(pw + kWarps * (nPix + 1));  // kWarps x (nPix+1): row values
+    RowMap *rm = reinterpret_cast<RowMap *>(vw + kWarps * (nPix + 1));  // kWarps (16-byte aligned: kWarps % 4 == 0)
+    float *dm = reinterpret_cast<float *>(rm + kWarps);              // nDet+1
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned full = 0xffffffffu;
+    const ViewInfo vi = info[p];
+    for (int k = threadIdx.x; k <= nDet; k += kThreads) dm[k] = detm[(size_t)p * (nDet + 1) + k];
+    const int ngroups = (nDet + 31) / 32;
+    const int g0 = warp * ngroups / kWarps, g1 = (warp + 1) * ngroups / kWarps;  // g1 - g0 <= NG (host check)
+    float acc[NG];
+#pragma unroll
+    for (int i = 0; i < NG; i++) acc[i] = 0.f;
+    float2 *pre = pw + warp * (nPix + 1);
+    float *val = vw + warp * (nPix + 1);
+    const int chunk = ((nPix + 1 + 31) / 32) | 1;  // prefix entries per lane (odd: conflict-free reads)
+    const int c_begin = min(nPix + 1, lane * chunk), c_end = min(nPix + 1, c_begin + chunk);
+    const int r_begin = blockIdx.y * rows_per_cta, r_end = min(nPix, r_begin + rows_per_cta);
+    const float qmax = (float)nPix;
+    for (int rb = r_begin; rb < r_end; rb += kWarps) {
+        __syncthreads();
+        // stage kWarps rows (as bdd_project_kernel)
+        if (vi.axis) {
+            const int total = kWarps * nPix;
+            for (int i0 = threadIdx.x; i0 < total; i0 += kStageU * kThreads) {
+                float v[kStageU];
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int i = i0 + u * kThreads, r = rb + i % kWarps;
+                    v[u] = (i < total && r < r_end) ? __ldg(phantom + r + (size_t)nPix * (i / kWarps)) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int i = i0 + u * kThreads;
+                    if (i < total) vw[(i % kWarps) * (nPix + 1) + i / kWarps] = v[u];
+                }
+            }
+        } else {
+            const int r = rb + warp;
+            const float *src = phantom + (size_t)nPix * r + (nPix - 1);
+            for (int c0 = lane; c0 < nPix; c0 += kStageU * 32) {
+                float v[kStageU];
+#pragma unroll
+                for (int u = 0; u < kStageU; u++) {
+                    const int c = c0 + 32 * u;
+                    v[u] = (c < nPix && r < r_end) ? __ldg(src - c) : 0.f;
+                }
+#pragma unroll
+                for (int u = 0; u < kStageU; u++)
+                    if (c0 + 32 * u < nPix) val[c0 + 32 * u] = v[u];
+            }
+        }
+        if (threadIdx.x < kWarps) vw[threadIdx.x * (nPix + 1) + nPix] = 0.f;
+        __syncthreads();
+        // this warp's row: two-float prefix (as bdd_project_kernel) and its boundary map
+        {
+            float th = 0.f, tl = 0.f;
+            for (int c = c_begin; c < c_end; c++) two_sum_add(th, tl, val[c]);
+            for (int off = 1; off < 32; off <<= 1) {
+                const float oh = __shfl_up_sync(full, th, off), ol = __shfl_up_sync(full, tl, off);
+                if (lane >= off) {
+                    two_sum_add(th, tl, oh);
+                    tl += ol;
+                }
+            }
+            float sh = __shfl_up_sync(full, th, 1), sl = __shfl_up_sync(full, tl, 1);
+            if (lane == 0) sh = sl = 0.f;
+            for (int c = c_begin; c < c_end; c++) {
+                pre[c] = make_float2(sh, sl);
+                two_sum_add(sh, sl, val[c]);
+            }
+            if (lane == 0) {
+                double r0d, deltad;
+                row_affine(vi, min(rb + warp, nPix - 1), nPix, G.pSize, &r0d, &deltad);
+                rm[warp] = RowMap{(float)r0d, (float)(1.0 / deltad), (float)std::fabs(deltad), 0.f};
+            }
+        }
+        __syncthreads();
+        // this warp's bins over the staged rows, in ascending row order
+        const int nrows = min(kWarps, r_end - rb);
+        for (int j = 0; j < nrows; j++) {
+            const RowMap m = rm[j];
+            const float2 *pj = pw + j * (nPix + 1);
+            const float *vj = vw + j * (nPix + 1);
+            auto F = [&](int k, float &fh, float &fl) {  // :98, as bdd_project_kernel
+                const float q = fminf(fmaxf((dm[k] - m.r0) * m.rdelta, 0.f), qmax);
+                const float mq = __fadd_rd(q, 8388608.f);
+                const int c = __float_as_int(mq) - 0x4B000000;
+                const float2 e = pj[c];
+                fh = e.x;
+                fl = fmaf(q - (mq - 8388608.f), vj[c], e.y);
+            };
+            float ch, cl;
+            F(min(g0 * 32 + lane, nDet), ch, cl);
+#pragma unroll
+            for (int i = 0; i < NG; i++) {
+                if (g0 + i < g1) {  // warp-uniform
+                    const int k0 = (g0 + i) * 32;
+                    float nh, nl;
+                    F(min(k0 + 32 + lane, nDet), nh, nl);
+                    float uh = __shfl_down_sync(full, ch, 1), ul = __shfl_down_sync(full, cl, 1);
+                    const float h0 = __shfl_sync(full, nh, 0), l0 = __shfl_sync(full, nl, 0);
+                    if (lane == 31) {
+                        uh = h0;
+                        ul = l0;
+                    }
+                    acc[i] += fabsf((uh - ch) + (ul - cl)) * m.adelta;  // :98-101
+                    ch = nh;
+                    cl = nl;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < NG; i++) {
+        const int n = (g0 + i) * 32 + lane;
+        if (g0 + i < g1 && n < nDet) atomicAdd(sino + p + (size_t)G.na * n, acc[i] * L[(size_t)p * nDet + n]);  // :104
+    }
+}
+
 // ------------------------------------------------------------------ backward
 // words per warp of the back-projector's skewed pixel accumulators (pixel c at c + c / 16)
 __host__ __device__ __forceinline__ int back_acc_pitch(int nPix) { return nPix + nPix / 16 + 1; }
@@ -430,6 +567,10 @@ size_t project_smem(const BddArgs &G) {
     return (sizeof(float2) + sizeof(float)) * (size_t)kWarps * (G.nPix + 1) +
            sizeof(float) * ((size_t)(G.nDet + 1) + (size_t)kWarps * G.nDet);
 }
+size_t project_bins_smem(const BddArgs &G) {
+    return (sizeof(float2) + sizeof(float)) * (size_t)kWarps * (G.nPix + 1) + sizeof(RowMap) * kWarps +
+           sizeof(float) * (size_t)(G.nDet + 1);
+}
 size_t back_smem(const BddArgs &G) {
     return sizeof(float4) * (size_t)back_tab_slots(G.nDet) + sizeof(float) * 2 * (size_t)kWarps * back_acc_pitch(G.nPix);
 }
@@ -480,6 +621,19 @@ int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino,
     int rows = (G.nPix + rsplit - 1) / rsplit;
     rows = (rows + kWarps - 1) / kWarps * kWarps;
     rsplit = (G.nPix + rows - 1) / rows;
+    // bins split over the warps (sums in registers) while each warp's range fits NG groups of 32
+    const int ngroups = (G.nDet + 31) / 32;
+    if (ngroups <= kWarps * 8) {
+        const size_t sb = project_bins_smem(G);
+        if (ngroups <= kWarps * 4) {
+            SGB_CUDA(cudaFuncSetAttribute(bdd_project_bins_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+            bdd_project_bins_kernel<4><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, phantom, sino, rows);
+        } else {
+            SGB_CUDA(cudaFuncSetAttribute(bdd_project_bins_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
+            bdd_project_bins_kernel<8><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, phantom, sino, rows);
+        }
+        return after_launch("bdd_project_bins_kernel");
+    }
     SGB_CUDA(cudaFuncSetAttribute(bdd_project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bdd_project_kernel<<<dim3(G.na, rsplit), kThreads, smem, st>>>(G, info, detm, L, phantom, sino, rows);
     return after_launch("bdd_project_kernel");

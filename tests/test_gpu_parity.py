@@ -301,6 +301,24 @@ def test_bdd_pair_against_oracle_and_adjoint(cuda, arc):
         assert O.rel_rmse(S.project_bdd(x, flat), Ax) > 1e-3
 
 
+@pytest.mark.parametrize("npix,ndet", [(60, 40), (300, 1024), (300, 1025), (500, 2200)])
+def test_bdd_project_bin_split_sizes(cuda, npix, ndet):
+    """The projector splits the bins over the warps in groups of 32 (at most 4 per warp up to
+    1024 bins, 8 up to 2048) and otherwise splits the rows: every split, warps without bins,
+    the last group partial and image rows that do not fill the last block of 8, against the FP64
+    oracle, per call and through a BddPlan.  Bins of 1.03 mm under 1 mm pixels (magnification
+    1.75), the ratio of the reference's test geometry; the image's shadow spans several warps'
+    bin ranges."""
+    import torch
+    angle = np.linspace(0.1, 2 * np.pi + 0.1, 12, endpoint=False)
+    geo = S.BddGeo(949.0, 541.0, 1.0, 1.03, npix, ndet, angle)
+    ogeo = O.bdd_geo(geo.DSD, geo.DS0, geo.pSize, geo.dSize, geo.nPix, geo.nDet, geo.angle)
+    x = np.random.default_rng(ndet).random((npix, npix)).astype(np.float32)
+    Ax = S.project_bdd(x, geo)
+    close(Ax, O.project_bdd(x, ogeo))
+    close(S.BddPlan(geo).project(torch.as_tensor(x, device="cuda")).cpu().numpy(), Ax, rmse=1e-6, maxrel=1e-6)
+
+
 def test_bdd_oversized_image_is_an_argument_error(cuda):
     """The projection's shared-memory tiles bound nPix (2012 at nDet = 888): a larger image is
     refused with an argument error before any launch."""
