@@ -573,6 +573,10 @@ def measure_2d(args):
             "judge_kept_learned": f"{kept}/8", "weights": os.path.basename(LF.default_weights_path()),
             "ms_learned_ramp_fbp": ms_ramp, "rmse_vs_phantom_learned_ramp": float(np.mean(rr)),
             "judge_kept_learned_ramp": f"{kept_r}/8", "ramp_gain": os.path.basename(LF.default_ramp_path())}
+        ms_train, _ = _lf_train_step_ms(10)
+        out["learned_filter_arc_888x90"]["train_step_ms"] = ms_train
+        out["learned_filter_arc_888x90"]["train_step"] = ("LearnedFilter.train_step on 4096 rows x 888 (forward, "
+                                                          "backward, Adam), CUDA-synchronised wall time, mean of 10")
     except Exception as e:  # the headline line must still print
         out["error"] = f"{type(e).__name__}: {e}"
     return out
@@ -752,6 +756,36 @@ def run_dd_case(args):
                       "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
 
 
+def _lf_train_step_ms(steps):
+    """Training step of the learned filter at the training script's batch: 4096 seeded rows of a
+    64-scan training set of the SinoFanArc 888 x 90 workload (888 samples per row), 3 + `steps`
+    calls of LearnedFilter.train_step; (CUDA-synchronised wall time per step in ms, last loss)."""
+    import torch
+
+    from sinograms import learned as LF
+    rg, ig = LF.sparse_fan_geometry()
+    zn, zc = LF.make_dataset(64, seed=3, rg=rg, ig=ig)
+    scale = float(zc.pow(2).mean().sqrt())
+    lf = LF.LearnedFilter(scale=scale, seed=1)
+    idx = torch.randperm(zn.shape[0], device="cuda", generator=torch.Generator(device="cuda").manual_seed(0))[:4096]
+    a, b = zn[idx].contiguous(), zc[idx].contiguous()
+    for _ in range(3):
+        lf.train_step(a, b, 1e-3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        loss = lf.train_step(a, b, 1e-3)
+    torch.cuda.synchronize()
+    return (time.perf_counter() - t0) / steps * 1e3, float(loss)
+
+
+def run_lf_train_case(args):
+    """The learned filter's training step (see _lf_train_step_ms), --steps timed calls."""
+    ms, loss = _lf_train_step_ms(args.steps)
+    print(json.dumps({"case": "lf_train_arc888x90_4096rows", "train_step_ms": ms, "rows": 4096, "L": 888,
+                      "steps": args.steps, "loss": loss}))
+
+
 def run_fbp2d_case(args):
     """The three 2D workloads for a back-projector capture: SinoPar 256 x 180 -> 256^2 (Hann),
     SinoFanArc 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
@@ -792,6 +826,8 @@ def run_case(args):
         return run_dd_case(args)
     if args.case == "fbp-2d":
         return run_fbp2d_case(args)
+    if args.case == "lf-train":
+        return run_lf_train_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -814,7 +850,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d"],
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d", "lf-train"],
                     help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"], help="storage form for --case")
     args = ap.parse_args()

@@ -9,10 +9,13 @@
 // Training kernels (hand-written; BF16 weights, FP32 activations and accumulation):
 //   conv32_tc     the 32 -> 32 layers' forward (+ bias, GELU) and data gradient (transposed,
 //                 flipped weights) on the tcgen05 tensor cores (see the comment above it)
+//   wgrad32_tc    the 32 -> 32 layers' weight and bias gradients on the tensor cores, with
+//                 wgrad_reduce adding the per-CTA partial sums in order
 //   conv_fwd      y[r,co,t] = b[co] + sum_{ci,k} W[co,ci,k] x[r,ci,t+k-4]  (+ GELU), SIMT, for
 //                 the 1 -> 32 layer and the last layer's data gradient
 //   conv_fwd_c1   the same for one output channel
-//   conv_wgrad    dW[co,ci,k] = sum_{r,t} g[r,co,t] x[r,ci,t+k-4], db[co] = sum g
+//   conv_wgrad    dW[co,ci,k] = sum_{r,t} g[r,co,t] x[r,ci,t+k-4], db[co] = sum g, SIMT, for the
+//                 1 -> 32 and 32 -> 1 layers
 //   gelu_bwd, loss (MSE on the residual), adam
 // Activations are (rows, channels, L) with L = detector samples, zero padded by 4.
 //
@@ -56,16 +59,27 @@ __device__ __forceinline__ float gelu_grad(float x) {
     const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
     return cdf + x * pdf;
 }
+// gelu(x) and gelu_grad(x), bit for bit, from one erf: the training forward stores the
+// derivative for the backward pass instead of the pre-activation.
+__device__ __forceinline__ void gelu_fwd(float x, float &g, float &d) {
+    const float e = erff(x * 0.70710678118654752f);
+    g = 0.5f * x * (1.f + e);
+    d = 0.5f * (1.f + e) + x * (0.39894228040143268f * __expf(-0.5f * x * x));
+}
 
 // ------------------------------------------------------------------ forward
 constexpr int kT = 128;          // positions per CTA
 constexpr int kCoPer = 4, kTPer = 8;
 
+// y[r, co, t] for kT positions of one row: thread (cg, tg) computes channels 4 cg .. 4 cg + 3 at
+// positions t0 + tg + 16 i (i < 8), so the 16 lanes of a channel store 16 consecutive positions.
+// With ACT it stores GELU(y) and, for the backward pass, GELU'(y).
 template <int CIN, int COUT, bool ACT, bool BIAS>
 __global__ void __launch_bounds__(128) conv_fwd(const float *__restrict__ in, const __nv_bfloat16 *__restrict__ W,
-                                                const float *__restrict__ b, float *__restrict__ pre,
+                                                const float *__restrict__ b, float *__restrict__ dg,
                                                 float *__restrict__ out, int L) {
     static_assert(COUT % kCoPer == 0 && (COUT / kCoPer) * (kT / kTPer) == 128, "thread mapping");
+    constexpr int kLanes = kT / kTPer;       // positions side by side (16)
     extern __shared__ float sm[];
     float *xs = sm;                          // [CIN][kT + 8]
     float *ws = xs + CIN * (kT + 2 * kPad);  // [COUT][CIN][9]
@@ -79,75 +93,98 @@ __global__ void __launch_bounds__(128) conv_fwd(const float *__restrict__ in, co
     }
     for (int i = threadIdx.x; i < COUT * CIN * kK; i += 128) ws[i] = __bfloat162float(W[i]);
     __syncthreads();
-    const int cg = threadIdx.x / (kT / kTPer), tg = threadIdx.x % (kT / kTPer);
-    const int co0 = cg * kCoPer, tl = tg * kTPer;
+    const int cg = threadIdx.x / kLanes, tg = threadIdx.x % kLanes;
+    const int co0 = cg * kCoPer;
     float acc[kCoPer][kTPer];
 #pragma unroll
     for (int j = 0; j < kCoPer; j++)
 #pragma unroll
         for (int i = 0; i < kTPer; i++) acc[j][i] = BIAS ? b[co0 + j] : 0.f;
     for (int ci = 0; ci < CIN; ci++) {
-        float xw[kTPer + kK - 1];
-#pragma unroll
-        for (int i = 0; i < kTPer + kK - 1; i++) xw[i] = xs[ci * (kT + 2 * kPad) + tl + i];
 #pragma unroll
         for (int k = 0; k < kK; k++) {
             float w[kCoPer];
 #pragma unroll
             for (int j = 0; j < kCoPer; j++) w[j] = ws[((co0 + j) * CIN + ci) * kK + k];
 #pragma unroll
-            for (int j = 0; j < kCoPer; j++)
+            for (int i = 0; i < kTPer; i++) {
+                const float xv = xs[ci * (kT + 2 * kPad) + tg + kLanes * i + k];
 #pragma unroll
-                for (int i = 0; i < kTPer; i++) acc[j][i] = fmaf(w[j], xw[i + k], acc[j][i]);
+                for (int j = 0; j < kCoPer; j++) acc[j][i] = fmaf(w[j], xv, acc[j][i]);
+            }
         }
     }
 #pragma unroll
     for (int j = 0; j < kCoPer; j++)
 #pragma unroll
         for (int i = 0; i < kTPer; i++) {
-            const int t = t0 + tl + i;
+            const int t = t0 + tg + kLanes * i;
             if (t >= L) continue;
             const long long o = (r * COUT + co0 + j) * (long long)L + t;
             if (ACT) {
-                pre[o] = acc[j][i];
-                out[o] = gelu(acc[j][i]);
+                float g, d;
+                gelu_fwd(acc[j][i], g, d);
+                dg[o] = d;
+                out[o] = g;
             } else {
                 out[o] = acc[j][i];
             }
         }
 }
 
-// one output channel (the last layer): a thread per position
+// one output channel (the last layer): a thread per position, the CTA's CIN x (128 + 8) inputs
+// staged in shared memory first
 template <int CIN>
 __global__ void __launch_bounds__(128) conv_fwd_c1(const float *__restrict__ in, const __nv_bfloat16 *__restrict__ W,
                                                    const float *__restrict__ b, float *__restrict__ out, int L,
                                                    bool bias) {
     __shared__ float ws[CIN * kK];
+    __shared__ float xs[CIN][128 + 2 * kPad];
     for (int i = threadIdx.x; i < CIN * kK; i += blockDim.x) ws[i] = __bfloat162float(W[i]);
-    __syncthreads();
     const long long r = blockIdx.y;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= L) return;
+    const int t0 = blockIdx.x * 128;
     const float *x = in + r * CIN * (long long)L;
+    // eight loads in flight per thread before their stores
+    constexpr int kRow = 128 + 2 * kPad, kTot = CIN * kRow;
+    for (int i0 = threadIdx.x; i0 < kTot; i0 += 8 * 128) {
+        float v[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int i = i0 + u * 128, t = t0 + i % kRow - kPad;
+            v[u] = (i < kTot && t >= 0 && t < L) ? x[(long long)(i / kRow) * L + t] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (i0 + u * 128 < kTot) xs[(i0 + u * 128) / kRow][(i0 + u * 128) % kRow] = v[u];
+    }
+    __syncthreads();
+    const int t = t0 + threadIdx.x;
+    if (t >= L) return;
     float acc = bias ? b[0] : 0.f;
     for (int ci = 0; ci < CIN; ci++)
 #pragma unroll
-        for (int k = 0; k < kK; k++) {
-            const int tt = t + k - kPad;
-            if (tt >= 0 && tt < L) acc = fmaf(ws[ci * kK + k], x[(long long)ci * L + tt], acc);
-        }
+        for (int k = 0; k < kK; k++) acc = fmaf(ws[ci * kK + k], xs[ci][threadIdx.x + k], acc);
     out[r * (long long)L + t] = acc;
 }
 
 // -------------------------------------------------------------- weight grad
 constexpr int kWT = 128;  // positions per tile
 
+// For the 1 -> 32 and 32 -> 1 layers (32 (co, ci) pairs): each warp takes a slice of 16 of the
+// tile's 128 positions and each lane one pair, so all 256 threads work; the eight slices' sums
+// are added in shared memory in slice order at the end.  Shared rows have odd length, so lanes
+// reading different channels at the same position fall in different banks.
 template <int CIN, int COUT>
 __global__ void __launch_bounds__(256) conv_wgrad(const float *__restrict__ in, const float *__restrict__ g,
                                                   float *__restrict__ dW, float *__restrict__ db, int L, long long R) {
-    constexpr int kPairsPer = (CIN * COUT + 255) / 256;  // (co, ci) pairs per thread
-    __shared__ float xs[CIN][kWT + 2 * kPad];
-    __shared__ float gs[COUT][kWT];
+    constexpr int kPairs = CIN * COUT;
+    constexpr int kSlices = kPairs >= 256 ? 1 : 256 / kPairs;  // position slices of a tile
+    constexpr int kPairsPer = kSlices == 1 ? (kPairs + 255) / 256 : 1;
+    constexpr int kSpan = kWT / kSlices;
+    static_assert(kSlices == 1 || (256 % kPairs == 0 && kWT % kSlices == 0), "slices");
+    __shared__ float xs[CIN][kWT + 2 * kPad + 1];
+    __shared__ float gs[COUT][kWT + 1];
+    __shared__ float red[kSlices > 1 ? kSlices * kPairs * (kK + 1) : 1];
     float acc[kPairsPer][kK];
     float bacc[kPairsPer];
 #pragma unroll
@@ -156,32 +193,47 @@ __global__ void __launch_bounds__(256) conv_wgrad(const float *__restrict__ in, 
 #pragma unroll
         for (int k = 0; k < kK; k++) acc[p][k] = 0.f;
     }
+    const int slice = kSlices == 1 ? 0 : (int)threadIdx.x / kPairs;
     const int tiles_per_row = (L + kWT - 1) / kWT;
     const long long ntiles = R * tiles_per_row;
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const long long r = tile / tiles_per_row;
         const int t0 = (int)(tile % tiles_per_row) * kWT;
         __syncthreads();
-        for (int i = threadIdx.x; i < CIN * (kWT + 2 * kPad); i += 256) {
-            const int ci = i / (kWT + 2 * kPad), j = i % (kWT + 2 * kPad);
-            const int t = t0 + j - kPad;
-            xs[ci][j] = (t >= 0 && t < L) ? in[(r * CIN + ci) * (long long)L + t] : 0.f;
+        // eight loads in flight per thread before their stores
+        constexpr int kXRow = kWT + 2 * kPad, kXTot = CIN * kXRow, kGTot = COUT * kWT;
+        for (int i0 = threadIdx.x; i0 < kXTot; i0 += 8 * 256) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * 256, t = t0 + i % kXRow - kPad;
+                v[u] = (i < kXTot && t >= 0 && t < L) ? in[(r * CIN + i / kXRow) * (long long)L + t] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (i0 + u * 256 < kXTot) xs[(i0 + u * 256) / kXRow][(i0 + u * 256) % kXRow] = v[u];
         }
-        for (int i = threadIdx.x; i < COUT * kWT; i += 256) {
-            const int co = i / kWT, j = i % kWT;
-            const int t = t0 + j;
-            gs[co][j] = (t < L) ? g[(r * COUT + co) * (long long)L + t] : 0.f;
+        for (int i0 = threadIdx.x; i0 < kGTot; i0 += 8 * 256) {
+            float v[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int i = i0 + u * 256, t = t0 + i % kWT;
+                v[u] = (i < kGTot && t < L) ? g[(r * COUT + i / kWT) * (long long)L + t] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (i0 + u * 256 < kGTot) gs[(i0 + u * 256) / kWT][(i0 + u * 256) % kWT] = v[u];
         }
         __syncthreads();
 #pragma unroll
         for (int p = 0; p < kPairsPer; p++) {
-            const int pair = threadIdx.x + 256 * p;
-            if (pair >= CIN * COUT) break;
-            const int co = pair / CIN, ci = pair % CIN;
+            const int pair = kSlices == 1 ? (int)threadIdx.x + 256 * p : (int)threadIdx.x % kPairs;
+            if (pair >= kPairs) break;
+            const int co = pair / CIN, ci = pair % CIN, j0 = slice * kSpan;
             float win[kK];
 #pragma unroll
-            for (int k = 0; k < kK - 1; k++) win[k] = xs[ci][k];
-            for (int j = 0; j < kWT; j++) {
+            for (int k = 0; k < kK - 1; k++) win[k] = xs[ci][j0 + k];
+            for (int j = j0; j < j0 + kSpan; j++) {
                 win[kK - 1] = xs[ci][j + kK - 1];
                 const float gv = gs[co][j];
 #pragma unroll
@@ -192,10 +244,29 @@ __global__ void __launch_bounds__(256) conv_wgrad(const float *__restrict__ in, 
             }
         }
     }
+    if (kSlices > 1) {
+        const int pair = (int)threadIdx.x % kPairs;
+        float *rs = red + (slice * kPairs + pair) * (kK + 1);
+#pragma unroll
+        for (int k = 0; k < kK; k++) rs[k] = acc[0][k];
+        rs[kK] = bacc[0];
+        __syncthreads();
+        if (slice == 0) {
+#pragma unroll
+            for (int k = 0; k <= kK; k++) {
+                float v = 0.f;
+                for (int q = 0; q < kSlices; q++) v += red[(q * kPairs + pair) * (kK + 1) + k];
+                if (k < kK) acc[0][k] = v;
+                else bacc[0] = v;
+            }
+        } else {
+            return;
+        }
+    }
 #pragma unroll
     for (int p = 0; p < kPairsPer; p++) {
-        const int pair = threadIdx.x + 256 * p;
-        if (pair >= CIN * COUT) break;
+        const int pair = kSlices == 1 ? (int)threadIdx.x + 256 * p : (int)threadIdx.x % kPairs;
+        if (pair >= kPairs) break;
         const int co = pair / CIN, ci = pair % CIN;
 #pragma unroll
         for (int k = 0; k < kK; k++) atomicAdd(dW + (co * CIN + ci) * kK + k, acc[p][k]);
@@ -204,9 +275,10 @@ __global__ void __launch_bounds__(256) conv_wgrad(const float *__restrict__ in, 
 }
 
 // ------------------------------------------------------------- elementwise
-__global__ void gelu_bwd(float *__restrict__ g, const float *__restrict__ pre, long long n) {
+// through a GELU in the backward pass: g *= GELU'(pre), the derivative stored by the forward
+__global__ void gelu_bwd(float *__restrict__ g, const float *__restrict__ dg, long long n) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        g[i] *= gelu_grad(pre[i]);
+        g[i] *= dg[i];
 }
 
 // residual MSE: net output o, input z, target y (all (R, L)); loss = mean((z + s o - y)^2)/s^2
@@ -480,7 +552,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
 // the SIMT passes keep them; each staged value is split into three BF16 pieces (hi, mid, lo:
 // 24 significant bits, the FP32 value) and the weights are the network's BF16 weights, so the
 // products are exact and D accumulates them in FP32.  The epilogue adds the bias and writes
-// the pre-activation and GELU(pre) (forward) or the plain sum (data gradient).
+// GELU(y) and GELU'(y) (forward, `pre` receives the derivative for the backward pass) or the
+// data gradient; given the stored GELU' of the layer below (`pre` not null), the data gradient
+// is taken through that layer's GELU too, so no separate pass over the gradient is needed.
 constexpr int kTrPieces = 3;
 constexpr int kTrThreads = 128;  // 4 warps: warp w owns TMEM lanes 32w .. 32w+31 (positions)
 constexpr int kTrABytes = kTrPieces * (kC / 8) * kTPos * 16;
@@ -524,29 +598,42 @@ __global__ void __launch_bounds__(kTrThreads) conv32_tc(const float *__restrict_
         const int t0 = (int)(tile % tpr) * kTM;
         const float *x = in + r * kC * (long long)L;
         // stage positions p = 0 .. 135 (t = t0 - 4 + p) of the 32 channels: one item is one
-        // position and one group of 8 channels; consecutive threads take consecutive positions
-        for (int idx = tid; idx < kTPos * (kC / 8); idx += kTrThreads) {
-            const int pp = idx % kTPos, cg = idx / kTPos;
-            const int t = t0 - kPad + pp;
-            const bool in_row = t >= 0 && t < L;
-            uint32_t h[kTrPieces][4];
+        // position and one group of 8 channels; consecutive threads take consecutive positions.
+        // Two items per pass, their 16 loads issued before any conversion.
+        for (int idx0 = tid; idx0 < kTPos * (kC / 8); idx0 += 2 * kTrThreads) {
+            float a[2][8];
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                float a0 = in_row ? __ldg(x + (long long)(cg * 8 + 2 * j) * L + t) : 0.f;
-                float a1 = in_row ? __ldg(x + (long long)(cg * 8 + 2 * j + 1) * L + t) : 0.f;
+            for (int u = 0; u < 2; u++) {
+                const int idx = idx0 + u * kTrThreads;
+                const int pp = idx % kTPos, cg = idx / kTPos;
+                const int t = t0 - kPad + pp;
+                const bool ok = idx < kTPos * (kC / 8) && t >= 0 && t < L;
 #pragma unroll
-                for (int pc = 0; pc < kTrPieces; pc++) {
-                    const __nv_bfloat162 v = __floats2bfloat162_rn(a0, a1);
-                    const float2 vf = __bfloat1622float2(v);
-                    h[pc][j] = *reinterpret_cast<const uint32_t *>(&v);
-                    a0 -= vf.x;
-                    a1 -= vf.y;
-                }
+                for (int e = 0; e < 8; e++) a[u][e] = ok ? __ldg(x + (long long)(cg * 8 + e) * L + t) : 0.f;
             }
 #pragma unroll
-            for (int pc = 0; pc < kTrPieces; pc++)
-                *reinterpret_cast<uint4 *>(A + ((pc * (kC / 8) + cg) * kTPos + pp) * 16) =
-                    make_uint4(h[pc][0], h[pc][1], h[pc][2], h[pc][3]);
+            for (int u = 0; u < 2; u++) {
+                const int idx = idx0 + u * kTrThreads;
+                if (idx >= kTPos * (kC / 8)) break;
+                const int pp = idx % kTPos, cg = idx / kTPos;
+                uint32_t h[kTrPieces][4];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    float a0 = a[u][2 * j], a1 = a[u][2 * j + 1];
+#pragma unroll
+                    for (int pc = 0; pc < kTrPieces; pc++) {
+                        const __nv_bfloat162 v = __floats2bfloat162_rn(a0, a1);
+                        const float2 vf = __bfloat1622float2(v);
+                        h[pc][j] = *reinterpret_cast<const uint32_t *>(&v);
+                        a0 -= vf.x;
+                        a1 -= vf.y;
+                    }
+                }
+#pragma unroll
+                for (int pc = 0; pc < kTrPieces; pc++)
+                    *reinterpret_cast<uint4 *>(A + ((pc * (kC / 8) + cg) * kTPos + pp) * 16) =
+                        make_uint4(h[pc][0], h[pc][1], h[pc][2], h[pc][3]);
+            }
         }
         tc::fence_proxy_async_smem();
         __syncthreads();
@@ -583,14 +670,17 @@ __global__ void __launch_bounds__(kTrThreads) conv32_tc(const float *__restrict_
             if (t < L) {
                 float *o = out + r * kC * (long long)L + t;
                 float *q = ACT ? pre + r * kC * (long long)L + t : nullptr;
+                const float *gp = !ACT && pre ? pre + r * kC * (long long)L + t : nullptr;
 #pragma unroll
                 for (int co = 0; co < kC; co++) {
                     const float a = v[co] + bias[co];
                     if (ACT) {
-                        q[(long long)co * L] = a;
-                        o[(long long)co * L] = gelu(a);
+                        float ga, da;
+                        gelu_fwd(a, ga, da);
+                        q[(long long)co * L] = da;
+                        o[(long long)co * L] = ga;
                     } else {
-                        o[(long long)co * L] = a;
+                        o[(long long)co * L] = gp ? a * gp[(long long)co * L] : a;
                     }
                 }
             }
@@ -601,6 +691,222 @@ __global__ void __launch_bounds__(kTrThreads) conv32_tc(const float *__restrict_
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tbase, 32);
+}
+
+// The 32 -> 32 layers' weight gradient on tcgen05:
+//   dW[co, ci, k] = sum_{r, t} G[r, co, t] X[r, ci, t + k - 4],   db[co] = sum_{r, t} G[r, co, t],
+// one chunk of 128 positions t of one row r at a time, the positions being the GEMM's K.
+// Both operands are staged in the MN-major no-swizzle layout (16 bytes = 8 channels of one
+// position per row, 8 positions per core matrix), so a shift of the positions by one is a
+// 16-byte shift of the start address.  M = 128 rows are (copy j, ci) over four copies of X
+// shifted by j = 0..3 positions, so one MMA covers taps t0 + j for t0 = 0, 4, 8 (taps 9-11 of
+// the last group are computed and dropped); N = the 32 channels co of G.  X and G are FP32
+// split into BF16 (hi, lo); the products hi.hi, hi.lo and lo.hi (16 significant bits of each
+// operand) accumulate in TMEM for one chunk, then into FP32 registers, so no accumulation chain
+// in the tensor core is longer than one chunk.  Each CTA writes its sums to its own slice of a
+// partial buffer, and wgrad_reduce adds the slices in CTA order: the result is deterministic.
+constexpr int kWgPos = 128;                 // positions per chunk (the GEMM's K)
+constexpr int kWgRows = kWgPos + 8;         // rows per shifted copy of X (taps up to 11)
+constexpr int kWgStage = kWgRows + 3;       // staged positions of X per chunk
+constexpr int kWgThreads = 128;             // warp w reads TMEM lanes 32w.. = copy j = w
+constexpr int kWgABytes = 2 * 4 * (kC / 8) * kWgRows * 16;  // [piece][copy][cg][row][8]
+constexpr int kWgBBytes = 2 * (kC / 8) * kWgPos * 16;       // [piece][cg][row][8]
+constexpr size_t kWgSmem = (size_t)kWgABytes + kWgBBytes + sizeof(float) * 4 * kC + 64;
+constexpr int kWgPart = kK * kC * kC + kC;  // floats per CTA slice: dW (k, co, ci), then db
+
+// MN-major no-swizzle descriptor: core matrices of 8 rows (K) x 16 bytes (8 MN elements);
+// K-adjacent core matrices lbo bytes apart, MN-adjacent ones sbo bytes apart.
+__device__ __forceinline__ uint64_t sdesc_mn_none(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+// eight FP32 values as (hi, lo) BF16 rows of 16 bytes
+__device__ __forceinline__ void split8(const float (&v)[8], uint4 &hi, uint4 &lo) {
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const __nv_bfloat162 a = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        const float2 af = __bfloat1622float2(a);
+        const __nv_bfloat162 b = __floats2bfloat162_rn(v[2 * j] - af.x, v[2 * j + 1] - af.y);
+        h[j] = *reinterpret_cast<const uint32_t *>(&a);
+        l[j] = *reinterpret_cast<const uint32_t *>(&b);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+__global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc(const float *__restrict__ x, const float *__restrict__ g,
+                                                             float *__restrict__ part, int L, long long R,
+                                                             int *err) {
+    extern __shared__ __align__(128) uint8_t wsm[];
+    uint8_t *A = wsm;               // X copies
+    uint8_t *B = A + kWgABytes;     // G
+    float *bred = reinterpret_cast<float *>(B + kWgBBytes);  // [warp][co] bias partial sums
+    uint64_t *bar = reinterpret_cast<uint64_t *>(((uintptr_t)(bred + 4 * kC) + 7) & ~uintptr_t(7));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        dev::mbar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 128);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *slot;
+    const uint32_t a_s = dev::smem_u32(A), b_s = dev::smem_u32(B);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(128, kC) | (1u << 15) | (1u << 16);  // A, B MN-major
+    float acc[3][kC];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int c = 0; c < kC; c++) acc[q][c] = 0.f;
+    float bsum[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // co = 8 (tid & 3) + e
+    const int cpr = (L + kWgPos - 1) / kWgPos;
+    const long long nchunks = R * cpr;
+    uint32_t phase = 0;
+    for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const long long r = ch / cpr;
+        const int p0 = (int)(ch % cpr) * kWgPos;
+        const float *xr = x + r * kC * (long long)L;
+        const float *gr = g + r * kC * (long long)L;
+        // X: staged position s is t = p0 - 4 + s; copy j row i holds s = i + j.  Two items per
+        // pass, their 16 loads issued before any conversion.
+        for (int idx0 = tid; idx0 < kWgStage * (kC / 8); idx0 += 2 * kWgThreads) {
+            float v[2][8];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int idx = idx0 + u * kWgThreads;
+                const int cg = idx & 3, s = idx >> 2;
+                const int t = p0 - kPad + s;
+                const bool in = idx < kWgStage * (kC / 8) && t >= 0 && t < L;
+#pragma unroll
+                for (int e = 0; e < 8; e++) v[u][e] = in ? __ldg(xr + (long long)(cg * 8 + e) * L + t) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int idx = idx0 + u * kWgThreads;
+                if (idx >= kWgStage * (kC / 8)) break;
+                const int cg = idx & 3, s = idx >> 2;
+                uint4 hi, lo;
+                split8(v[u], hi, lo);
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int i = s - j;
+                    if (i >= 0 && i < kWgRows) {
+                        *reinterpret_cast<uint4 *>(A + ((j * 4 + cg) * kWgRows + i) * 16) = hi;
+                        *reinterpret_cast<uint4 *>(A + (((4 + j) * 4 + cg) * kWgRows + i) * 16) = lo;
+                    }
+                }
+            }
+        }
+        // G: row i is t = p0 + i (each thread keeps one channel group, tid & 3); two items per pass
+        static_assert(kWgPos * (kC / 8) % (2 * kWgThreads) == 0, "whole passes over G");
+        for (int idx0 = tid; idx0 < kWgPos * (kC / 8); idx0 += 2 * kWgThreads) {
+            float v[2][8];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int t = p0 + ((idx0 + u * kWgThreads) >> 2);
+#pragma unroll
+                for (int e = 0; e < 8; e++) v[u][e] = t < L ? __ldg(gr + (long long)((tid & 3) * 8 + e) * L + t) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int cg = tid & 3, i = (idx0 + u * kWgThreads) >> 2;
+#pragma unroll
+                for (int e = 0; e < 8; e++) bsum[e] += v[u][e];
+                uint4 hi, lo;
+                split8(v[u], hi, lo);
+                *reinterpret_cast<uint4 *>(B + (cg * kWgPos + i) * 16) = hi;
+                *reinterpret_cast<uint4 *>(B + ((4 + cg) * kWgPos + i) * 16) = lo;
+            }
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        int good = 1;
+        if (tid == 0) {
+            tc::fence_after_sync();
+            constexpr int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};  // hi.hi, hi.lo, lo.hi
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                int n = 0;
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+#pragma unroll
+                    for (int ks = 0; ks < kWgPos / 16; ks++, n++) {
+                        const uint64_t ad = sdesc_mn_none(
+                            a_s + (uint32_t)((pa[c] * 4 * 4 * kWgRows + 4 * q + 16 * ks) * 16), 128, kWgRows * 16);
+                        const uint64_t bd =
+                            sdesc_mn_none(b_s + (uint32_t)((pb[c] * 4 * kWgPos + 16 * ks) * 16), 128, kWgPos * 16);
+                        tc::mma_bf16(tbase + 32 * q, ad, bd, idesc, n != 0);
+                    }
+            }
+            tc::commit(bar);
+            const long long c0 = clock64();
+            while (!dev::mbar_try_wait(bar, phase & 1))
+                if (clock64() - c0 > dev::kWaitBudget) {
+                    atomicOr(err, 1);
+                    good = 0;
+                    break;
+                }
+        }
+        good = __syncthreads_and(good);
+        phase++;
+        tc::fence_after_sync();
+        if (!good) break;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            float v[32];
+            tc::ld32(tbase + ((uint32_t)(32 * warp) << 16) + 32 * q, v);
+#pragma unroll
+            for (int c = 0; c < kC; c++) acc[q][c] += v[c];
+        }
+        tc::fence_before_sync();
+        __syncthreads();  // TMEM read and staging buffers free before the next chunk
+    }
+    // this CTA's slice: dW as (k, co, ci) with ci = lane, k = 4 q + warp; then db
+    float *ps = part + (long long)blockIdx.x * kWgPart;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const int k = 4 * q + warp;
+        if (k < kK)
+#pragma unroll
+            for (int c = 0; c < kC; c++) ps[(k * kC + c) * kC + lane] = acc[q][c];
+    }
+#pragma unroll
+    for (int e = 0; e < 8; e++) {  // lanes with equal tid & 3 hold the same channels
+        float s = bsum[e];
+        s += __shfl_xor_sync(0xffffffffu, s, 4);
+        s += __shfl_xor_sync(0xffffffffu, s, 8);
+        s += __shfl_xor_sync(0xffffffffu, s, 16);
+        bsum[e] = s;
+    }
+    if (lane < 4)
+#pragma unroll
+        for (int e = 0; e < 8; e++) bred[warp * kC + lane * 8 + e] = bsum[e];
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid < kC) ps[kK * kC * kC + tid] = ((bred[tid] + bred[kC + tid]) + bred[2 * kC + tid]) + bred[3 * kC + tid];
+    if (warp == 0) tc::tmem_dealloc(tbase, 128);
+}
+
+// dW[(co * 32 + ci) * 9 + k] += sum over the CTA slices in order; db[co] likewise.
+__global__ void wgrad_reduce(const float *__restrict__ part, int nslices, float *__restrict__ dW,
+                             float *__restrict__ db) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kWgPart) return;
+    float s = 0.f;
+    for (int c = 0; c < nslices; c++) s += part[(long long)c * kWgPart + i];
+    if (i < kK * kC * kC) {
+        const int k = i / (kC * kC), co = (i / kC) % kC, ci = i % kC;
+        dW[(co * kC + ci) * kK + k] += s;
+    } else {
+        db[i - kK * kC * kC] += s;
+    }
 }
 
 // Adam on the FP32 master parameters; refreshes the BF16 weights and the transposed,
@@ -651,7 +957,7 @@ struct sgb_lf {
     DevBuf p, g, m, v, wb, wt, loss;
     long long step = 0;
     // activation workspace (grown on demand)
-    DevBuf act[kLayers + 1], pre[kLayers], ga, gb, gz;
+    DevBuf act[kLayers + 1], dgl[kLayers], ga, gb, gz;  // dgl: GELU'(pre-activation) per hidden layer
     long long cap_rows = 0;
     int cap_L = 0;
     // tensor-core inference: packed weights of the 32 -> 32 layers (valid for twp_step), error flag
@@ -661,6 +967,8 @@ struct sgb_lf {
     // valid for trp_step
     DevBuf trp;
     long long trp_step = -1;
+    // tensor-core weight gradient: one slice of partial sums per CTA
+    DevBuf wpart;
 };
 
 namespace {
@@ -671,7 +979,7 @@ int lf_workspace(sgb_lf *F, long long R, int L) {
         const int ch = l == 0 ? 1 : (l == kLayers ? 1 : kC);
         SGB_TRY(F->act[l].reserve(sizeof(float) * (size_t)R * ch * L));
     }
-    for (int l = 0; l < kLayers - 1; l++) SGB_TRY(F->pre[l].reserve(sizeof(float) * (size_t)R * kC * L));
+    for (int l = 0; l < kLayers - 1; l++) SGB_TRY(F->dgl[l].reserve(sizeof(float) * (size_t)R * kC * L));
     SGB_TRY(F->ga.reserve(sizeof(float) * (size_t)R * kC * L));
     SGB_TRY(F->gb.reserve(sizeof(float) * (size_t)R * kC * L));
     SGB_TRY(F->gz.reserve(sizeof(float) * (size_t)R * L));
@@ -728,6 +1036,26 @@ int launch_conv32_tc(sgb_lf *F, const float *in, int slot, const float *b, float
     return after_launch("conv32_tc");
 }
 
+// dW, db (+=) of a 32 -> 32 layer from its input x and the gradient g at its pre-activation.
+int launch_wgrad32_tc(sgb_lf *F, const float *x, const float *g, float *dW, float *db, int L, long long R,
+                      cudaStream_t st) {
+    int dev = 0;
+    SGB_CUDA(cudaGetDevice(&dev));
+    static bool attr_done[64] = {};  // per device
+    if (dev < 0 || dev >= 64 || !attr_done[dev]) {
+        SGB_CUDA(cudaFuncSetAttribute(wgrad32_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWgSmem));
+        if (dev >= 0 && dev < 64) attr_done[dev] = true;
+    }
+    const long long nch = R * ((L + kWgPos - 1) / kWgPos);
+    if (nch <= 0) return SGB_OK;
+    const int grid = (int)std::min<long long>(nch, 2ll * num_sms());
+    SGB_TRY(F->wpart.reserve(sizeof(float) * (size_t)grid * kWgPart));
+    wgrad32_tc<<<grid, kWgThreads, kWgSmem, st>>>(x, g, F->wpart.as<float>(), L, R, F->terr.as<int>());
+    SGB_TRY(after_launch("wgrad32_tc"));
+    wgrad_reduce<<<(kWgPart + 255) / 256, 256, 0, st>>>(F->wpart.as<float>(), grid, dW, db);
+    return after_launch("wgrad_reduce");
+}
+
 // forward through the 5 layers; act[0] must hold z/s; result (net output) in act[5].  Layers 1-3
 // (32 -> 32) on the tensor cores, the 1 -> 32 and 32 -> 1 layers in SIMT.
 int lf_forward(sgb_lf *F, long long R, int L, cudaStream_t st) {
@@ -735,9 +1063,9 @@ int lf_forward(sgb_lf *F, long long R, int L, cudaStream_t st) {
     const float *p = F->p.as<float>();
     SGB_TRY(lf_train_weights(F, st));
     SGB_TRY((launch_conv<1, kC, true, true>(F->act[0].as<float>(), wb + F->wbase[0], p + F->off.b[0],
-                                            F->pre[0].as<float>(), F->act[1].as<float>(), L, R, st)));
+                                            F->dgl[0].as<float>(), F->act[1].as<float>(), L, R, st)));
     for (int l = 1; l < kLayers - 1; l++)
-        SGB_TRY((launch_conv32_tc<true, true>(F, F->act[l].as<float>(), l - 1, p + F->off.b[l], F->pre[l].as<float>(),
+        SGB_TRY((launch_conv32_tc<true, true>(F, F->act[l].as<float>(), l - 1, p + F->off.b[l], F->dgl[l].as<float>(),
                                               F->act[l + 1].as<float>(), L, R, st)));
     conv_fwd_c1<kC><<<dim3((L + 127) / 128, (unsigned)R), 128, 0, st>>>(
         F->act[kLayers - 1].as<float>(), wb + F->wbase[kLayers - 1], p + F->off.b[kLayers - 1],
@@ -787,7 +1115,7 @@ int lf_backward(sgb_lf *F, long long R, int L, cudaStream_t st) {
     const __nv_bfloat16 *wt = F->wt.as<__nv_bfloat16>();
     float *g = F->g.as<float>();
     SGB_CUDA(cudaMemsetAsync(g, 0, sizeof(float) * F->nparam, st));
-    const unsigned wgrid = 2 * 152;
+    const unsigned wgrid = 6 * std::max(1, num_sms());  // six 256-thread CTAs per SM hide the staging latency
     // layer 5 (32 -> 1): weight grad, data grad into ga (32 channels)
     conv_wgrad<kC, 1><<<wgrid, 256, 0, st>>>(F->act[4].as<float>(), F->gz.as<float>(), g + F->off.w[4],
                                              g + F->off.b[4], L, R);
@@ -795,23 +1123,18 @@ int lf_backward(sgb_lf *F, long long R, int L, cudaStream_t st) {
     SGB_TRY((launch_conv<1, kC, false, false>(F->gz.as<float>(), wt + F->wbase[4], nullptr, nullptr,
                                               F->ga.as<float>(), L, R, st)));
     float *gcur = F->ga.as<float>(), *gnext = F->gb.as<float>();
-    for (int l = kLayers - 2; l >= 0; l--) {
-        // through GELU of layer l
-        gelu_bwd<<<grid_for(R * kC * (long long)L), 256, 0, st>>>(gcur, F->pre[l].as<float>(), R * kC * (long long)L);
-        SGB_TRY(after_launch("gelu_bwd"));
-        if (l == 0) {
-            conv_wgrad<1, kC><<<wgrid, 256, 0, st>>>(F->act[0].as<float>(), gcur, g + F->off.w[0], g + F->off.b[0], L,
-                                                      R);
-            SGB_TRY(after_launch("conv_wgrad"));
-        } else {
-            conv_wgrad<kC, kC><<<wgrid, 256, 0, st>>>(F->act[l].as<float>(), gcur, g + F->off.w[l], g + F->off.b[l],
-                                                       L, R);
-            SGB_TRY(after_launch("conv_wgrad"));
-            SGB_TRY((launch_conv32_tc<false, false>(F, gcur, l + 2, nullptr, nullptr, gnext, L, R, st)));
-            std::swap(gcur, gnext);
-        }
+    // through GELU of layer 3; the data-gradient passes below take the gradient through the
+    // GELU of the layer beneath in their epilogue
+    gelu_bwd<<<grid_for(R * kC * (long long)L), 256, 0, st>>>(gcur, F->dgl[kLayers - 2].as<float>(),
+                                                              R * kC * (long long)L);
+    SGB_TRY(after_launch("gelu_bwd"));
+    for (int l = kLayers - 2; l >= 1; l--) {
+        SGB_TRY(launch_wgrad32_tc(F, F->act[l].as<float>(), gcur, g + F->off.w[l], g + F->off.b[l], L, R, st));
+        SGB_TRY((launch_conv32_tc<false, false>(F, gcur, l + 2, nullptr, F->dgl[l - 1].as<float>(), gnext, L, R, st)));
+        std::swap(gcur, gnext);
     }
-    return SGB_OK;
+    conv_wgrad<1, kC><<<wgrid, 256, 0, st>>>(F->act[0].as<float>(), gcur, g + F->off.w[0], g + F->off.b[0], L, R);
+    return after_launch("conv_wgrad");
 }
 
 int lf_refresh(sgb_lf *F, cudaStream_t st) {

@@ -37,6 +37,27 @@ def test_gradients_match_fp64_oracle(cuda, L):
     assert np.abs(y - yo).max() <= 5e-5 * np.abs(yo).max()
 
 
+@pytest.mark.parametrize("rows,L", [(24, 888), (5, 302)])
+def test_weight_gradients_per_layer_match_fp64_oracle(cuda, rows, L):
+    """Each layer's weight and bias gradient against the FP64 oracle, separately: the three
+    32 -> 32 layers' weight gradients run on the tensor cores (operands split hi+lo in BF16,
+    a partial sum per CTA), the others in SIMT.  Rows of several 128-position chunks, the last
+    one partial."""
+    rng = np.random.default_rng(rows * 1000 + L)
+    p = (0.2 * rng.standard_normal(LO.nparams())).astype(np.float32)
+    z = rng.standard_normal((rows, L)).astype(np.float32)
+    t = rng.standard_normal((rows, L)).astype(np.float32)
+    lf = LF.LearnedFilter(scale=0.9, params=p)
+    _, g = lf.loss_grad(z, t)
+    _, go = LO.loss_grad(p.astype(np.float64), z, t, 0.9, bf16_weights=True)
+    o = 0
+    for ci, co in zip(LO.CIN, LO.COUT):
+        for n in (co * ci * LO.K, co):
+            a, b = g[o:o + n], go[o:o + n]
+            assert np.linalg.norm(a - b) / np.linalg.norm(b) < 1e-4, (ci, co, n)
+            o += n
+
+
 @pytest.mark.parametrize("rows,L", [(3, 37), (130, 200), (90, 888)])
 def test_tensor_core_apply_matches_fp64_oracle(cuda, rows, L):
     """The inference forward (32 -> 32 layers on tcgen05, activations split hi+lo in BF16)
