@@ -18,10 +18,11 @@ namespace fdkdev {
 // follow the same item sequence through the one mbarrier ring.  A DONE tag ends the CTA.
 constexpr int kDone = -1;
 
-// Register budget: three CTAs per SM for short z-runs; ZU = 64 keeps the compiler's own choice
-// (measured: bounding it to two CTAs slowed the 32-wide ZU 64 launch of the 48-scan workload 8%)
+// Register budget: three CTAs per SM for short z-runs; ZU = 64 with FP32 pairs keeps the
+// compiler's own choice (measured: bounding it to two CTAs slowed the 32-wide ZU 64 launch of the
+// 48-scan workload 8%), ZU = 64 with FP16 quads is bounded to two CTAs like the single-scan kernel
 template <typename TP, int ZU, int BW, int VPS, int NSTAGE>
-__global__ void __launch_bounds__(kThreads, (ZU == 64 ? 1 : kFdkMinCtas<ZU, VPS>))
+__global__ void __launch_bounds__(kThreads, ((ZU == 64 && !kQuad<TP>) ? 1 : kFdkMinCtas<ZU, VPS>))
     fdk_tma_batch_kernel(FdkBatchArgs B, const __grid_constant__ FdkBatchMaps maps) {
     extern __shared__ __align__(128) unsigned char smraw[];
     unsigned char *sm = smraw + ((128 - (smem_u32(smraw) & 127)) & 127);
