@@ -894,6 +894,194 @@ __global__ void __launch_bounds__(kWgThreads, 2) wgrad32_tc(const float *__restr
     if (warp == 0) tc::tmem_dealloc(tbase, 128);
 }
 
+// wgrad32_tc with TMA staging, for rows whose length L is a multiple of 4 (16-byte row
+// strides), in chunks of 64 positions so that two CTAs of 4 warps share an SM.  Thread 0 brings
+// each chunk's FP32 tiles into one of two slots with cp.async.bulk.tensor, one chunk ahead: X as
+// 32 channels x 76 positions from t = p0 - 4, G as 32 x 64 from t = p0 (positions outside
+// [0, L) read as zeros).  The threads split the tiles into the BF16 operands (the layout and MMAs
+// of wgrad32_tc with 72 rows per shifted copy) and read the TMEM sums as wgrad32_tc does.
+constexpr int kWtPos = 64;                 // positions per chunk
+constexpr int kWtRows = kWtPos + 8;        // rows per shifted copy of X
+constexpr int kWtBox = kWtPos + 12;        // staged positions of X: 76, 304-byte rows
+constexpr int kWtXBytes = kC * kWtBox * 4;
+constexpr int kWtGBytes = kC * kWtPos * 4;
+constexpr int kWtSlot = kWtXBytes + kWtGBytes;
+constexpr int kWtABytes = 2 * 4 * (kC / 8) * kWtRows * 16;
+constexpr int kWtBBytes = 2 * (kC / 8) * kWtPos * 16;
+constexpr size_t kWtSmem = 128 + 2 * (size_t)kWtSlot + kWtABytes + kWtBBytes + sizeof(float) * 4 * kC + 64;
+static_assert(kWtXBytes % 128 == 0 && kWtSlot % 128 == 0 && kWtABytes % 128 == 0, "TMA and operand alignment");
+
+__global__ void __launch_bounds__(kWgThreads, 2)
+    wgrad32_tma(const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap gmap,
+                float *__restrict__ part, int L, long long R, int *err) {
+    extern __shared__ uint8_t wraw[];
+    // 128-byte aligned by pointer arithmetic on the shared array, so accesses stay ld/st.shared
+    uint8_t *S = wraw + ((128u - (dev::smem_u32(wraw) & 127u)) & 127u);  // [2][X tile, G tile]
+    uint8_t *A = S + 2 * kWtSlot;
+    uint8_t *B = A + kWtABytes;
+    float *bred = reinterpret_cast<float *>(B + kWtBBytes);  // [warp][co]
+    uint64_t *full = reinterpret_cast<uint64_t *>(bred + 4 * kC);  // [2], then the MMA barrier
+    uint64_t *mbar = full + 2;
+    uint32_t *slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        dev::mbar_init(full, 1);
+        dev::mbar_init(full + 1, 1);
+        dev::mbar_init(mbar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 128);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = *slot;
+    const uint32_t a_s = dev::smem_u32(A), b_s = dev::smem_u32(B);
+    constexpr uint32_t idesc = tc::idesc_bf16_f32(128, kC) | (1u << 15) | (1u << 16);  // A, B MN-major
+    const int cpr = (L + kWtPos - 1) / kWtPos;
+    const long long nchunks = R * cpr;
+    auto issue = [&](long long ch, int sl) {  // thread 0: chunk ch's tiles into slot sl
+        const int r = (int)(ch / cpr), p0 = (int)(ch % cpr) * kWtPos;
+        dev::mbar_arrive_expect_tx(full + sl, kWtSlot);
+        dev::tma_load_3d(S + sl * kWtSlot, &xmap, p0 - kPad, 0, r, full + sl);
+        dev::tma_load_3d(S + sl * kWtSlot + kWtXBytes, &gmap, p0, 0, r, full + sl);
+    };
+    float acc[3][kC];
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+#pragma unroll
+        for (int c = 0; c < kC; c++) acc[q][c] = 0.f;
+    float bsum[2][8] = {};  // co = 8 (2 u + tid / 64) + e
+    if (tid == 0 && blockIdx.x < nchunks) issue(blockIdx.x, 0);
+    uint32_t inflight = blockIdx.x < nchunks ? 1u : 0u;  // slots with a load not yet waited for (bit sl)
+    int good = 1;
+    long long i = 0;
+    for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x, i++) {
+        const int sl = (int)(i & 1);
+        if (tid == 0 && ch + gridDim.x < nchunks) issue(ch + gridDim.x, sl ^ 1);  // its slot was read last pass
+        if (ch + gridDim.x < nchunks) inflight |= 1u << (sl ^ 1);
+        // this chunk's tiles (the slot's phase parity alternates every second chunk)
+        const int ok = dev::mbar_wait(full + sl, (uint32_t)((i >> 1) & 1));
+        if (ok) inflight &= ~(1u << sl);
+        if (!__syncthreads_and(ok)) {
+            if (tid == 0) atomicOr(err, 1);
+            good = 0;
+            break;
+        }
+        const float *xt = reinterpret_cast<const float *>(S + sl * kWtSlot);
+        const float *gt = reinterpret_cast<const float *>(S + sl * kWtSlot + kWtXBytes);
+        // X: staged position s (t = p0 - 4 + s) into the four shifted copies; positions vary
+        // fastest across the lanes, so the tile's rows (304 bytes apart) are read without bank
+        // conflicts and the copies' 16-byte rows are written without them
+        constexpr int kNS = kWtRows + 3;
+        for (int idx = tid; idx < kNS * (kC / 8); idx += kWgThreads) {
+            const int s = idx % kNS, cg = idx / kNS;
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) v[e] = xt[(cg * 8 + e) * kWtBox + s];
+            uint4 hi, lo;
+            split8(v, hi, lo);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int r = s - j;
+                if (r >= 0 && r < kWtRows) {
+                    *reinterpret_cast<uint4 *>(A + ((j * 4 + cg) * kWtRows + r) * 16) = hi;
+                    *reinterpret_cast<uint4 *>(A + (((4 + j) * 4 + cg) * kWtRows + r) * 16) = lo;
+                }
+            }
+        }
+        // G: row p (t = p0 + p), positions fastest; pass u takes channel group 2 u + tid / 64
+        static_assert(kWtPos * (kC / 8) == 2 * kWgThreads && kWtPos == 64, "two passes over G");
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            const int p = tid & (kWtPos - 1), cg = 2 * u + (tid >> 6);
+            float v[8];
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                v[e] = gt[(cg * 8 + e) * kWtPos + p];
+                bsum[u][e] += v[e];
+            }
+            uint4 hi, lo;
+            split8(v, hi, lo);
+            *reinterpret_cast<uint4 *>(B + (cg * kWtPos + p) * 16) = hi;
+            *reinterpret_cast<uint4 *>(B + ((4 + cg) * kWtPos + p) * 16) = lo;
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();  // operands staged; the slot is free for the load after next
+        int mok = 1;
+        if (tid == 0) {
+            tc::fence_after_sync();
+            constexpr int pa[3] = {0, 0, 1}, pb[3] = {0, 1, 0};  // hi.hi, hi.lo, lo.hi
+#pragma unroll
+            for (int q = 0; q < 3; q++) {
+                int n = 0;
+#pragma unroll
+                for (int c = 0; c < 3; c++)
+#pragma unroll
+                    for (int ks = 0; ks < kWtPos / 16; ks++, n++) {
+                        const uint64_t ad = sdesc_mn_none(
+                            a_s + (uint32_t)((pa[c] * 4 * 4 * kWtRows + 4 * q + 16 * ks) * 16), 128, kWtRows * 16);
+                        const uint64_t bd =
+                            sdesc_mn_none(b_s + (uint32_t)((pb[c] * 4 * kWtPos + 16 * ks) * 16), 128, kWtPos * 16);
+                        tc::mma_bf16(tbase + 32 * q, ad, bd, idesc, n != 0);
+                    }
+            }
+            tc::commit(mbar);
+            if (!dev::mbar_wait(mbar, (uint32_t)(i & 1))) {
+                atomicOr(err, 1);
+                mok = 0;
+            }
+        }
+        if (!__syncthreads_and(mok)) {
+            good = 0;
+            break;
+        }
+        tc::fence_after_sync();
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            float v[32];
+            tc::ld32(tbase + ((uint32_t)(32 * warp) << 16) + 32 * q, v);
+#pragma unroll
+            for (int c = 0; c < kC; c++) acc[q][c] += v[c];
+        }
+        tc::fence_before_sync();
+        __syncthreads();  // TMEM read and operand buffers free before the next chunk
+    }
+    // a load issued ahead and never waited for (an early exit) must land before the CTA ends
+    if (tid == 0)
+        for (int sl = 0; sl < 2; sl++)
+            if (inflight & (1u << sl)) {
+                const long long k = i + (sl != (int)(i & 1) ? 1 : 0);
+                if (!dev::mbar_wait(full + sl, (uint32_t)((k >> 1) & 1))) atomicOr(err, 1);
+            }
+    float *ps = part + (long long)blockIdx.x * kWgPart;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const int k = 4 * q + warp;
+        if (k < kK)
+#pragma unroll
+            for (int c = 0; c < kC; c++) ps[(k * kC + c) * kC + lane] = good ? acc[q][c] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 2; u++)  // all lanes of a warp hold the same channels
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            float s = bsum[u][e];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) bred[warp * 16 + u * 8 + e] = s;  // warp w: groups 2 u + w / 2
+        }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid < kC) {  // channel group cg = 2 u + w / 2 comes from warps 2 (cg & 1) and 2 (cg & 1) + 1
+        const int cg = tid >> 3, u = cg >> 1, w0 = 2 * (cg & 1), e = tid & 7;
+        ps[kK * kC * kC + tid] = bred[w0 * 16 + u * 8 + e] + bred[(w0 + 1) * 16 + u * 8 + e];
+    }
+    if (warp == 0) tc::tmem_dealloc(tbase, 128);
+}
+
 // dW[(co * 32 + ci) * 9 + k] += sum over the CTA slices in order; db[co] likewise.
 __global__ void wgrad_reduce(const float *__restrict__ part, int nslices, float *__restrict__ dW,
                              float *__restrict__ db) {
@@ -1048,10 +1236,41 @@ int launch_wgrad32_tc(sgb_lf *F, const float *x, const float *g, float *dW, floa
     }
     const long long nch = R * ((L + kWgPos - 1) / kWgPos);
     if (nch <= 0) return SGB_OK;
-    const int grid = (int)std::min<long long>(nch, 2ll * num_sms());
-    SGB_TRY(F->wpart.reserve(sizeof(float) * (size_t)grid * kWgPart));
-    wgrad32_tc<<<grid, kWgThreads, kWgSmem, st>>>(x, g, F->wpart.as<float>(), L, R, F->terr.as<int>());
-    SGB_TRY(after_launch("wgrad32_tc"));
+    int grid;
+    PFN_cuTensorMapEncodeTiled_v12000 enc = L % 4 == 0 ? encode_fn() : nullptr;
+    if (enc) {  // TMA staging: rows of whole 16-byte units
+        static bool tattr_done[64] = {};
+        if (dev < 0 || dev >= 64 || !tattr_done[dev]) {
+            SGB_CUDA(cudaFuncSetAttribute(wgrad32_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWtSmem));
+            if (dev >= 0 && dev < 64) tattr_done[dev] = true;
+        }
+        CUtensorMap xm, gm;
+        const void *ptr[2] = {x, g};
+        CUtensorMap *maps[2] = {&xm, &gm};
+        const cuuint32_t boxx[2] = {(cuuint32_t)kWtBox, (cuuint32_t)kWtPos};
+        for (int m = 0; m < 2; m++) {
+            cuuint64_t dims[3] = {(cuuint64_t)L, (cuuint64_t)kC, (cuuint64_t)R};
+            cuuint64_t strides[2] = {(cuuint64_t)L * 4, (cuuint64_t)kC * L * 4};
+            cuuint32_t box[3] = {boxx[m], (cuuint32_t)kC, 1};
+            cuuint32_t estr[3] = {1, 1, 1};
+            const CUresult r = enc(maps[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(ptr[m]), dims,
+                                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                set_error("wgrad32: cuTensorMapEncodeTiled failed (%d), L=%d", (int)r, L);
+                return SGB_ERR_CUDA;
+            }
+        }
+        grid = (int)std::min<long long>(R * ((L + kWtPos - 1) / kWtPos), 2ll * num_sms());
+        SGB_TRY(F->wpart.reserve(sizeof(float) * (size_t)grid * kWgPart));
+        wgrad32_tma<<<grid, kWgThreads, kWtSmem, st>>>(xm, gm, F->wpart.as<float>(), L, R, F->terr.as<int>());
+        SGB_TRY(after_launch("wgrad32_tma"));
+    } else {
+        grid = (int)std::min<long long>(nch, 2ll * num_sms());
+        SGB_TRY(F->wpart.reserve(sizeof(float) * (size_t)grid * kWgPart));
+        wgrad32_tc<<<grid, kWgThreads, kWgSmem, st>>>(x, g, F->wpart.as<float>(), L, R, F->terr.as<int>());
+        SGB_TRY(after_launch("wgrad32_tc"));
+    }
     wgrad_reduce<<<(kWgPart + 255) / 256, 256, 0, st>>>(F->wpart.as<float>(), grid, dW, db);
     return after_launch("wgrad_reduce");
 }
