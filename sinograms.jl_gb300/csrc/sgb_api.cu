@@ -1019,6 +1019,7 @@ int sgb_bdd_plan_create_det(int nPix, int nDet, int na, const double *angle, dou
     SGB_TRY(P->fwd.reserve(bdd_project_scratch(P->G)));
     SGB_TRY(P->back.reserve(bdd_back_scratch(P->G)));
     SGB_TRY(launch_bdd_project_setup(P->G, P->fwd.p, st));
+    SGB_TRY(launch_bdd_back_setup(P->G, P->back.p, st));
     SGB_CUDA(cudaStreamSynchronize(st));
     *out = P.release();
     return SGB_OK;
@@ -1056,7 +1057,7 @@ int sgb_bdd_plan_backproject(sgb_bdd_plan *P, const float *sino, float *image, i
         SGB_TRY(P->dout.reserve(nout * sizeof(float)));
         out_dev = P->dout.as<float>();
     }
-    SGB_TRY(launch_bdd_back(G, static_cast<const float *>(in_dev), out_dev, P->back.p, st));
+    SGB_TRY(launch_bdd_back_main(G, static_cast<const float *>(in_dev), out_dev, P->back.p, st));
     if (!(flags & SGB_DEVICE_PTRS))
         SGB_CUDA(cudaMemcpyAsync(image, out_dev, nout * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (flags & SGB_ASYNC) return SGB_OK;

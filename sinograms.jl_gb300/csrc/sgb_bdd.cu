@@ -108,16 +108,17 @@ __device__ __forceinline__ void row_affine(const ViewInfo &vi, int r, int nPix, 
 }
 
 // ------------------------------------------------------------ per-view set-up
-// forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info, the knot table T
-// (nDet+1 float4 per view: x = knot K[j] in ascending order, y = density B[j] / (K[j+1]-K[j])
-// of bin j, 0 for the last knot; z, w = the prefix, filled by bdd_prefix_kernel) and the
-// per-bin integrals B (nDet, ascending order: sino * L * |ddetm|, signed as the reference's
-// prefix, :196; reversed when detm descends, :198-202).
+// forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info and the geometry table
+// (nDet+1 float4 per view, in ascending knot order: x = knot K[j]; y = the integral of bin j per
+// unit sinogram value, L * |ddetm| signed as the reference's prefix, :196, and reversed when
+// detm descends, :198-202; z = the same per unit length, the bin's density factor; w of the last
+// knot = 1 when detm descends).  Both depend on the geometry only, so plans compute them once;
+// bdd_fill_prefix_kernel multiplies in the sinogram per call.
 // One CTA per (view, chunk of kSetupChunk bins): the view's constants once, each FP64 boundary
 // once into shared memory, then the chunk's outputs from those values (the same FP64 calls).
 constexpr int kSetupChunk = kThreads;
 __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo *info, float *detm, float *L,
-                                                             const float *sino, float4 *tab, float *kb) {
+                                                             float4 *geo) {
     __shared__ ViewInfo vis;
     __shared__ int desc_s;
     __shared__ double bnd[kSetupChunk + 1];
@@ -127,9 +128,9 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
     if (threadIdx.x == 0) {
         vis = view_info(beta, G.DS0);
         if (blockIdx.y == 0) info[p] = vis;
-        desc_s = sino ? det_boundary(vis, beta, 0, nDet, G.DSD, G.DS0, G.dSize, G.arc) >
-                            det_boundary(vis, beta, 1, nDet, G.DSD, G.DS0, G.dSize, G.arc)
-                      : 0;
+        desc_s = geo ? det_boundary(vis, beta, 0, nDet, G.DSD, G.DS0, G.dSize, G.arc) >
+                           det_boundary(vis, beta, 1, nDet, G.DSD, G.DS0, G.dSize, G.arc)
+                     : 0;
     }
     __syncthreads();
     const ViewInfo vi = vis;
@@ -139,29 +140,28 @@ __global__ void __launch_bounds__(kThreads) bdd_setup_kernel(BddArgs G, ViewInfo
     for (int i = threadIdx.x; i <= cnt; i += blockDim.x)
         bnd[i] = det_boundary(vi, beta, b0 + i, nDet, G.DSD, G.DS0, G.dSize, G.arc);
     __syncthreads();
-    if (!sino) {
+    if (!geo) {
         float *dm = detm + (size_t)p * (nDet + 1);
         for (int k = n0 + threadIdx.x; k <= n1; k += blockDim.x) dm[k] = (float)bnd[k - n0];
         for (int n = n0 + threadIdx.x; n < n1; n += blockDim.x)
             L[(size_t)p * nDet + n] = (float)det_scale(vi, bnd[n - n0], bnd[n + 1 - n0], G.pSize);
         return;
     }
-    float4 *T = tab + (size_t)p * (nDet + 1);
-    float *B = kb + (size_t)p * nDet;
+    float4 *T = geo + (size_t)p * (nDet + 1);
     // this chunk writes knots n0 .. n1-1 with their bins, and the last chunk also knot nDet
     for (int j = n0 + threadIdx.x; j < n1 || (j == nDet && n1 == nDet); j += blockDim.x) {
         // ascending knot j is reference boundary desc ? nDet-j : j; ascending bin j covers
         // reference bin n = desc ? nDet-1-j : j
         const int src = desc ? nDet - j : j;
-        float dens = 0.f;
+        float cb = 0.f, cd = 0.f;
         if (j < n1) {
             const int n = desc ? nDet - 1 - j : j;
             const double d0 = bnd[n - b0], d1 = bnd[n + 1 - b0];
-            const double w = ((double)sino[p + (size_t)G.na * n] * det_scale(vi, d0, d1, G.pSize)) * (d1 - d0);
-            B[j] = (float)(desc ? -w : w);  // integral over the bin in the ascending direction
-            dens = (float)((desc ? -w : w) / std::fabs(d1 - d0));
+            const double w = det_scale(vi, d0, d1, G.pSize) * (d1 - d0);
+            cb = (float)(desc ? -w : w);  // the bin's integral per unit sinogram value, ascending
+            cd = (float)((desc ? -w : w) / std::fabs(d1 - d0));  // and its density
         }
-        T[j] = make_float4((float)bnd[src - b0], dens, 0.f, 0.f);
+        T[j] = make_float4((float)bnd[src - b0], cb, cd, j == nDet ? (float)desc : 0.f);
     }
 }
 
@@ -441,39 +441,52 @@ __host__ __device__ __forceinline__ int back_acc_pitch(int nPix) { return nPix +
 // float4 slots of the swizzled knot table: nDet + 1 knots rounded up to whole groups of 8
 __host__ __device__ __forceinline__ int back_tab_slots(int nDet) { return (nDet + 1 + 7) / 8 * 8; }
 
-// Detector prefix integral of one view (integrate1D over the bins, :196): a warp-level scan of
-// the ascending bin integrals B in two-float arithmetic, P[0] = 0, P[j+1] = P[j] + B[j], written
-// into the knot table's (z, w) = (hi, lo).  One warp per view.
-__global__ void __launch_bounds__(kThreads) bdd_prefix_kernel(BddArgs G, const float *kb, float4 *tab) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int p = blockIdx.x * kWarps + warp;
-    if (p >= G.na) return;  // warp-uniform
-    const int nDet = G.nDet;
-    const float *B = kb + (size_t)p * nDet;
+// The back-projector's per-call table: one CTA per view forms each bin's integral B[j] =
+// sino * (geometry factor) and density, in ascending knot order, and the two-float prefix of B
+// over the knots (integrate1D, :229-241, of the weighted sinogram, :196), by a block-wide scan:
+// each thread sums a contiguous run of bins, the runs' totals are scanned within each warp by
+// shuffles and across the warps through shared memory, in order.  T[j] = (K[j], density of bin
+// j, prefix hi, prefix lo), T[nDet] = (K[nDet], 0, total).
+__global__ void __launch_bounds__(kThreads) bdd_fill_prefix_kernel(BddArgs G, const float *__restrict__ sino,
+                                                                  const float4 *__restrict__ geo, float4 *tab) {
+    __shared__ float2 wtot[kWarps];
+    const int p = blockIdx.x, nDet = G.nDet;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const float4 *Gv = geo + (size_t)p * (nDet + 1);
     float4 *T = tab + (size_t)p * (nDet + 1);
-    const unsigned full = 0xffffffffu;
-    const int chunk = (nDet + 31) / 32;
-    const int j_begin = min(nDet, lane * chunk), j_end = min(nDet, j_begin + chunk);
+    const bool desc = Gv[nDet].w != 0.f;
+    const int chunk = (nDet + kThreads - 1) / kThreads;
+    const int j_begin = min(nDet, tid * chunk), j_end = min(nDet, j_begin + chunk);
+    // B[j] of ascending bin j (reference bin desc ? nDet-1-j : j)
     float th = 0.f, tl = 0.f;
-    for (int j = j_begin; j < j_end; j++) two_sum_add(th, tl, B[j]);
-    for (int off = 1; off < 32; off <<= 1) {
+    for (int j = j_begin; j < j_end; j++)
+        two_sum_add(th, tl, sino[p + (size_t)G.na * (desc ? nDet - 1 - j : j)] * Gv[j].y);
+    const unsigned full = 0xffffffffu;
+    for (int off = 1; off < 32; off <<= 1) {  // inclusive scan of the runs within the warp
         const float oh = __shfl_up_sync(full, th, off), ol = __shfl_up_sync(full, tl, off);
         if (lane >= off) {
             two_sum_add(th, tl, oh);
             tl += ol;
         }
     }
-    float sh = __shfl_up_sync(full, th, 1), sl = __shfl_up_sync(full, tl, 1);
-    if (lane == 0) sh = sl = 0.f;
+    if (lane == 31) wtot[warp] = make_float2(th, tl);
+    __syncthreads();
+    float sh = 0.f, sl = 0.f;  // this run's start: the earlier warps, then the earlier lanes
+    for (int w = 0; w < warp; w++) {
+        two_sum_add(sh, sl, wtot[w].x);
+        sl += wtot[w].y;
+    }
+    float eh = __shfl_up_sync(full, th, 1), el = __shfl_up_sync(full, tl, 1);
+    if (lane == 0) eh = el = 0.f;
+    two_sum_add(sh, sl, eh);
+    sl += el;
     for (int j = j_begin; j < j_end; j++) {
-        T[j].z = sh;
-        T[j].w = sl;
-        two_sum_add(sh, sl, B[j]);
+        const float s = sino[p + (size_t)G.na * (desc ? nDet - 1 - j : j)];
+        const float4 g = Gv[j];
+        T[j] = make_float4(g.x, s * g.z, sh, sl);
+        two_sum_add(sh, sl, s * g.y);
     }
-    if (lane == 31) {
-        T[nDet].z = th;
-        T[nDet].w = tl;
-    }
+    if (j_begin < nDet && j_end == nDet) T[nDet] = make_float4(Gv[nDet].x, 0.f, sh, sl);
 }
 
 // Shared-memory slot of knot j: XOR-swizzled within groups of 8 float4 (the 32 banks), so lanes
@@ -582,7 +595,7 @@ size_t bdd_project_scratch(const BddArgs &G) {
 }
 
 size_t bdd_back_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + sizeof(float4) * (size_t)G.na * (G.nDet + 1) + sizeof(float) * (size_t)G.na * G.nDet;
+    return info_bytes(G.na) + 2 * sizeof(float4) * (size_t)G.na * (G.nDet + 1);  // info, knot table, geometry
 }
 
 int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
@@ -593,8 +606,8 @@ int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
     float *detm = reinterpret_cast<float *>(static_cast<char *>(scratch) + info_bytes(G.na));
     float *L = detm + (size_t)G.na * (G.nDet + 1);
-    bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L, nullptr,
-                                                                                             nullptr, nullptr);
+    bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L,
+                                                                                             nullptr);
     return after_launch("bdd_setup_kernel");
 }
 
@@ -639,21 +652,30 @@ int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino,
     return after_launch("bdd_project_kernel");
 }
 
-int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scratch, cudaStream_t st) {
-    size_t smem = back_smem(G);
-    if (smem > 220 * 1024) {
+int launch_bdd_back_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
+    if (back_smem(G) > 220 * 1024) {
         set_error("backproject_bdd: nPix=%d nDet=%d exceed the shared-memory tile", G.nPix, G.nDet);
         return SGB_ERR_ARG;
     }
     ViewInfo *info = static_cast<ViewInfo *>(scratch);
-    float4 *tab = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na));
-    float *kb = reinterpret_cast<float *>(tab + (size_t)G.na * (G.nDet + 1));
-    SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
+    float4 *geo = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na)) + (size_t)G.na * (G.nDet + 1);
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, nullptr, nullptr,
-                                                                                             sino, tab, kb);
-    SGB_TRY(after_launch("bdd_setup_kernel"));
-    bdd_prefix_kernel<<<(G.na + kWarps - 1) / kWarps, kThreads, 0, st>>>(G, kb, tab);
-    SGB_TRY(after_launch("bdd_prefix_kernel"));
+                                                                                             geo);
+    return after_launch("bdd_setup_kernel");
+}
+
+int launch_bdd_back_main(const BddArgs &G, const float *sino, float *image, void *scratch, cudaStream_t st) {
+    const size_t smem = back_smem(G);
+    if (smem > 220 * 1024) {
+        set_error("backproject_bdd: nPix=%d nDet=%d exceed the shared-memory tile", G.nPix, G.nDet);
+        return SGB_ERR_ARG;
+    }
+    const ViewInfo *info = static_cast<const ViewInfo *>(scratch);
+    float4 *tab = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na));
+    const float4 *geo = tab + (size_t)G.na * (G.nDet + 1);
+    SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
+    bdd_fill_prefix_kernel<<<G.na, kThreads, 0, st>>>(G, sino, geo, tab);
+    SGB_TRY(after_launch("bdd_fill_prefix_kernel"));
     int gx = (G.nPix + kWarps - 1) / kWarps;
     // views split over CTAs so that each SM holds ~8 of them (row blocks x view groups)
     const int target = 8 * std::max(1, num_sms());
@@ -663,6 +685,11 @@ int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scr
     SGB_CUDA(cudaFuncSetAttribute(bdd_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, tab, image, vpc);
     return after_launch("bdd_back_kernel");
+}
+
+int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scratch, cudaStream_t st) {
+    SGB_TRY(launch_bdd_back_setup(G, scratch, st));
+    return launch_bdd_back_main(G, sino, image, scratch, st);
 }
 
 }  // namespace sgb

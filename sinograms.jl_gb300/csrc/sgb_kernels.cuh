@@ -117,6 +117,10 @@ int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino,
 int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
                        cudaStream_t st);
 size_t bdd_back_scratch(const BddArgs &G);
+// backproject_bdd split the same way: the geometry table once, the sinogram's table and the
+// back-projection per call
+int launch_bdd_back_setup(const BddArgs &G, void *scratch, cudaStream_t st);
+int launch_bdd_back_main(const BddArgs &G, const float *sino, float *image, void *scratch, cudaStream_t st);
 int launch_bdd_back(const BddArgs &G, const float *sino, float *image, void *scratch,
                     cudaStream_t st);
 
