@@ -786,6 +786,29 @@ def run_lf_train_case(args):
                       "steps": args.steps, "loss": loss}))
 
 
+def run_lf_apply_case(args):
+    """Learned-filter inference on the 90-view scan: the plan's ramp-filtered rows of one seeded
+    phantom's noisy DD sinogram, then 3 + --steps calls of LearnedFilter.apply (one lf_tc_fused
+    launch each) enqueued back to back; mean time per call from CUDA events."""
+    import torch
+
+    import sinograms as S
+    from sinograms import learned as LF
+    rg, ig = LF.sparse_fan_geometry()
+    plan = S.plan_fbp(rg, ig)
+    lf = LF.LearnedFilter.load(LF.default_weights_path())
+    img = LF.ellipse_image(ig.with_mask(None), LF.phantom_ellipses(900000))
+    sino = LF.dd_project(img, S.BddGeo.from_geoms(rg, ig))
+    sino = sino + 0.005 * sino.abs().max() * torch.randn(sino.shape, device="cuda",
+                                                         generator=torch.Generator(device="cuda").manual_seed(7))
+    z = LF.fbp_filter_rows(plan, sino)
+    for _ in range(3):
+        lf.apply(z, sync=False)
+    ms = _per_call_ms(lambda: lf.apply(z, sync=False), args.steps)
+    print(json.dumps({"case": "lf_apply_arc888x90", "rows": int(z.shape[0]), "L": int(z.shape[1]),
+                      "ms_network": ms}))
+
+
 def run_fbp2d_case(args):
     """The three 2D workloads for a back-projector capture: SinoPar 256 x 180 -> 256^2 (Hann),
     SinoFanArc 888 x 90 views -> 512^2 (the learned-filter scan) and SinoFanArc 888 x 512 views
@@ -828,6 +851,8 @@ def run_case(args):
         return run_fbp2d_case(args)
     if args.case == "lf-train":
         return run_lf_train_case(args)
+    if args.case == "lf-apply":
+        return run_lf_apply_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -850,7 +875,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d", "lf-train"],
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d", "lf-train", "lf-apply"],
                     help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"], help="storage form for --case")
     args = ap.parse_args()

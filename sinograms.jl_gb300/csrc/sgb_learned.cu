@@ -324,8 +324,12 @@ __global__ void scale_copy(const float *__restrict__ a, float s, float *__restri
 // advanced by k positions (16 B), so one staged tile serves all nine taps.  The weights
 // are staged the same way, [tap][ch / 8][co][8].
 constexpr int kTM = 128, kTPos = kTM + 2 * kPad;
+// Rows per channel group in the inference kernel's activation buffers: one more than the tile's
+// positions, so the four channel groups of one position (2192 bytes apart) fall in different
+// shared-memory banks; the descriptors' leading byte offset carries the pitch.
+constexpr int kTPitch = kTPos + 1;
 constexpr int kTcThreads = 512;  // 16 warps: warp w reads TMEM lane quarter w % 4, channel group w / 4
-constexpr int kTcABytes = 2 * (kC / 8) * kTPos * 16;  // two pieces
+constexpr int kTcABytes = 2 * (kC / 8) * kTPitch * 16;  // two pieces
 constexpr int kTcWBytes = kK * (kC / 8) * kC * 16;
 
 __device__ __forceinline__ uint64_t sdesc_k_none(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -344,8 +348,8 @@ __device__ __forceinline__ void store_split8(uint8_t *A, int cg, int pos, const 
         h[j] = *reinterpret_cast<uint32_t *>(&a);
         l[j] = *reinterpret_cast<uint32_t *>(&b);
     }
-    *reinterpret_cast<uint4 *>(A + (cg * kTPos + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16) = make_uint4(l[0], l[1], l[2], l[3]);
+    *reinterpret_cast<uint4 *>(A + (cg * kTPitch + pos) * 16) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(A + ((kC / 8 + cg) * kTPitch + pos) * 16) = make_uint4(l[0], l[1], l[2], l[3]);
 }
 
 // channels 4 c4 .. 4 c4 + 3 of one position (half of channel group c4 / 2), split hi/lo
@@ -360,8 +364,8 @@ __device__ __forceinline__ void store_split4(uint8_t *A, int c4, int pos, const 
         l[j] = *reinterpret_cast<uint32_t *>(&b);
     }
     const int cg = c4 >> 1, half = (c4 & 1) * 8;
-    *reinterpret_cast<uint2 *>(A + (cg * kTPos + pos) * 16 + half) = make_uint2(h[0], h[1]);
-    *reinterpret_cast<uint2 *>(A + ((kC / 8 + cg) * kTPos + pos) * 16 + half) = make_uint2(l[0], l[1]);
+    *reinterpret_cast<uint2 *>(A + (cg * kTPitch + pos) * 16 + half) = make_uint2(h[0], h[1]);
+    *reinterpret_cast<uint2 *>(A + ((kC / 8 + cg) * kTPitch + pos) * 16 + half) = make_uint2(l[0], l[1]);
 }
 
 // where each layer's BF16 weights and FP32 bias start in the parameter arrays
@@ -431,14 +435,21 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
     const long long ntiles = R * tpr;
     uint32_t phase = 0;
     bool ok = true;
+    // z window value `tid` of a tile (t = ts - 20 + tid), loaded one tile ahead so that its
+    // latency overlaps the previous tile's work
+    static_assert(kFZ <= kTcThreads, "one window value per thread");
+    auto zload = [&](long long tl) -> float {
+        if (tid >= kFZ || tl >= ntiles) return 0.f;
+        const long long rr = tl / tpr;
+        const int t = (int)(tl % tpr) * kFOut - 20 + tid;
+        return (t >= 0 && t < L) ? z[rr * L + t] : 0.f;
+    };
+    float znext = zload(blockIdx.x);
     for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const long long r = tile / tpr;
         const int ts = (int)(tile % tpr) * kFOut;  // window position p <-> t = ts - 16 + p
-        const float *zr = z + r * L;
-        for (int j = tid; j < kFZ; j += kTcThreads) {
-            const int t = ts - 20 + j;
-            zw[j] = (t >= 0 && t < L) ? zr[t] : 0.f;
-        }
+        if (tid < kFZ) zw[tid] = znext;
+        znext = zload(tile + gridDim.x);
         __syncthreads();
         // layer 0 (1 -> 32, GELU) on all 136 window positions, into buffer 0: one item per
         // (position, 4 output channels), half a 16-byte channel-group row
@@ -464,7 +475,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
             if (tid == 0) {
                 tc::fence_after_sync();
                 // descriptors advance by start address only (bits 0-13 hold address / 16)
-                const uint64_t a0 = sdesc_k_none(ab0 + cur * kTcABytes, kTPos * 16, 128);
+                const uint64_t a0 = sdesc_k_none(ab0 + cur * kTcABytes, kTPitch * 16, 128);
                 const uint64_t b0 = sdesc_k_none(wl0 + l * kTcWBytes, kC * 16, 128);
                 int n = 0;
 #pragma unroll
@@ -473,7 +484,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
                     for (int k = 0; k < kK; k++)
 #pragma unroll
                         for (int ks = 0; ks < kC / 16; ks++, n++) {
-                            const uint64_t ad = a0 + (uint64_t)((piece * (kC / 8) + 2 * ks) * kTPos + k);
+                            const uint64_t ad = a0 + (uint64_t)((piece * (kC / 8) + 2 * ks) * kTPitch + k);
                             const uint64_t bd = b0 + (uint64_t)((k * (kC / 8) + 2 * ks) * kC);
                             tc::mma_bf16(tbase, ad, bd, idesc, n != 0);
                         }
@@ -501,10 +512,10 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
                 for (int j = 0; j < 8; j++) v[j] = (t >= 0 && t < L) ? gelu_infer(v[j] + bl[j]) : 0.f;
                 store_split8(Ab + (cur ^ 1) * kTcABytes, cg, pp, v);
             }
-            if (!__syncthreads_and(good)) ok = false;  // also orders the TMEM reads before the next MMAs
+            // this thread's operand stores and TMEM reads, ordered before the next layer's MMAs
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
-            __syncthreads();
+            if (!__syncthreads_and(good)) ok = false;
         }
         if (!ok) break;
         // last layer (32 -> 1) and the residual on the 104 exact positions
@@ -518,8 +529,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) lf_tc_fused(const float *__rest
 #pragma unroll
             for (int k = 0; k < kK; k++) {
                 const int row = pp - 4 + k;
-                const uint4 h = *reinterpret_cast<const uint4 *>(A + (cg * kTPos + row) * 16);
-                const uint4 q = *reinterpret_cast<const uint4 *>(A + ((kC / 8 + cg) * kTPos + row) * 16);
+                const uint4 h = *reinterpret_cast<const uint4 *>(A + (cg * kTPitch + row) * 16);
+                const uint4 q = *reinterpret_cast<const uint4 *>(A + ((kC / 8 + cg) * kTPitch + row) * 16);
                 const uint32_t hv[4] = {h.x, h.y, h.z, h.w}, qv[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
