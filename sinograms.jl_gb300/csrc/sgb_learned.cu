@@ -38,33 +38,34 @@ __host__ __device__ constexpr int cin_of(int l) { return l == 0 ? 1 : kC; }
 __host__ __device__ constexpr int cout_of(int l) { return l == kLayers - 1 ? 1 : kC; }
 __host__ __device__ constexpr int wcount(int l) { return cout_of(l) * cin_of(l) * kK; }
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
-// Inference GELU x Phi(x), with erf by Abramowitz & Stegun 7.1.26 (Hastings' rational form,
+// GELU x Phi(x) with erf by Abramowitz & Stegun 7.1.26 (Hastings' rational form,
 // |error| <= 1.5e-7): Phi(-|x|) = 0.5 P(t) exp(-u^2), u = |x| / sqrt 2, t = 1 / (1 + 0.3275911 u),
-// and Phi(|x|) = 1 - Phi(-|x|).  Branch-free, one reciprocal and one exp2; it differs from the
-// training GELU (erff) by ~1e-7, far below the network's BF16 weight precision.
-__device__ __forceinline__ float gelu_infer(float x) {
+// and Phi(|x|) = 1 - Phi(-|x|).  Branch-free, one reciprocal and one exp2.  Returns Phi(x) and
+// exp(-x^2 / 2).
+__device__ __forceinline__ float phi_as(float x, float &e) {
     const float u = fabsf(x) * 0.70710678118654752f;
-    float t, e;
+    float t;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(t) : "f"(fmaf(0.3275911f, u, 1.f)));
     // 0.5 * (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5)
     const float hp =
         t * fmaf(t, fmaf(t, fmaf(t, fmaf(t, 0.5307027145f, -0.7265760135f), 0.7107068705f), -0.142248368f), 0.127414796f);
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(-u * u * 1.4426950408889634f));
     const float h = hp * e;  // Phi(-|x|)
-    return x * (x >= 0.f ? 1.f - h : h);
+    return x >= 0.f ? 1.f - h : h;
 }
-__device__ __forceinline__ float gelu_grad(float x) {
-    const float cdf = 0.5f * (1.f + erff(x * 0.70710678118654752f));
-    const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-    return cdf + x * pdf;
+// Inference GELU; it differs from the exact-erf GELU by ~1e-7, far below the network's BF16
+// weight precision.
+__device__ __forceinline__ float gelu_infer(float x) {
+    float e;
+    return x * phi_as(x, e);
 }
-// gelu(x) and gelu_grad(x), bit for bit, from one erf: the training forward stores the
+// Training GELU and its derivative Phi(x) + x phi(x) from the same terms: the forward stores the
 // derivative for the backward pass instead of the pre-activation.
 __device__ __forceinline__ void gelu_fwd(float x, float &g, float &d) {
-    const float e = erff(x * 0.70710678118654752f);
-    g = 0.5f * x * (1.f + e);
-    d = 0.5f * (1.f + e) + x * (0.39894228040143268f * __expf(-0.5f * x * x));
+    float e;
+    const float p = phi_as(x, e);
+    g = x * p;
+    d = fmaf(x, 0.39894228040143268f * e, p);
 }
 
 // ------------------------------------------------------------------ forward
@@ -1217,6 +1218,32 @@ int lf_train_weights(sgb_lf *F, cudaStream_t st) {
     return SGB_OK;
 }
 
+// Tensor map of channel-major activations (R rows x 32 channels x L positions, FP32) read in
+// boxes of box_x positions x 32 channels; positions outside [0, L) read as zeros.  Needs L % 4 == 0
+// (16-byte row strides).
+int encode_rows32(const float *p, int L, long long R, int box_x, CUtensorMap *map) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = encode_fn();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return SGB_ERR_CUDA;
+    }
+    cuuint64_t dims[3] = {(cuuint64_t)L, (cuuint64_t)kC, (cuuint64_t)R};
+    cuuint64_t strides[2] = {(cuuint64_t)L * 4, (cuuint64_t)kC * L * 4};
+    cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)kC, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(p), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("learned filter: cuTensorMapEncodeTiled failed (%d), L=%d", (int)r, L);
+        return SGB_ERR_CUDA;
+    }
+    return SGB_OK;
+}
+
+// TMA staging when the rows are whole 16-byte units (L % 4 == 0) and the driver offers tensor maps
+bool tma_rows_ok(int L) { return L % 4 == 0 && encode_fn() != nullptr; }
+
 template <bool ACT, bool BIAS>
 int launch_conv32_tc(sgb_lf *F, const float *in, int slot, const float *b, float *pre, float *out, int L, long long R,
                      cudaStream_t st) {
@@ -1248,30 +1275,15 @@ int launch_wgrad32_tc(sgb_lf *F, const float *x, const float *g, float *dW, floa
     const long long nch = R * ((L + kWgPos - 1) / kWgPos);
     if (nch <= 0) return SGB_OK;
     int grid;
-    PFN_cuTensorMapEncodeTiled_v12000 enc = L % 4 == 0 ? encode_fn() : nullptr;
-    if (enc) {  // TMA staging: rows of whole 16-byte units
+    if (tma_rows_ok(L)) {  // TMA staging: rows of whole 16-byte units
         static bool tattr_done[64] = {};
         if (dev < 0 || dev >= 64 || !tattr_done[dev]) {
             SGB_CUDA(cudaFuncSetAttribute(wgrad32_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kWtSmem));
             if (dev >= 0 && dev < 64) tattr_done[dev] = true;
         }
         CUtensorMap xm, gm;
-        const void *ptr[2] = {x, g};
-        CUtensorMap *maps[2] = {&xm, &gm};
-        const cuuint32_t boxx[2] = {(cuuint32_t)kWtBox, (cuuint32_t)kWtPos};
-        for (int m = 0; m < 2; m++) {
-            cuuint64_t dims[3] = {(cuuint64_t)L, (cuuint64_t)kC, (cuuint64_t)R};
-            cuuint64_t strides[2] = {(cuuint64_t)L * 4, (cuuint64_t)kC * L * 4};
-            cuuint32_t box[3] = {boxx[m], (cuuint32_t)kC, 1};
-            cuuint32_t estr[3] = {1, 1, 1};
-            const CUresult r = enc(maps[m], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(ptr[m]), dims,
-                                   strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                   CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-            if (r != CUDA_SUCCESS) {
-                set_error("wgrad32: cuTensorMapEncodeTiled failed (%d), L=%d", (int)r, L);
-                return SGB_ERR_CUDA;
-            }
-        }
+        SGB_TRY(encode_rows32(x, L, R, kWtBox, &xm));
+        SGB_TRY(encode_rows32(g, L, R, kWtPos, &gm));
         grid = (int)std::min<long long>(R * ((L + kWtPos - 1) / kWtPos), 2ll * num_sms());
         SGB_TRY(F->wpart.reserve(sizeof(float) * (size_t)grid * kWgPart));
         wgrad32_tma<<<grid, kWgThreads, kWtSmem, st>>>(xm, gm, F->wpart.as<float>(), L, R, F->terr.as<int>());
