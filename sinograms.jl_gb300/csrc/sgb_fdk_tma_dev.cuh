@@ -191,23 +191,27 @@ __device__ __forceinline__ ColView view_setup(const FdkTmaArgs &A, float x, floa
     if (g.hi < g.lo) return g;
     // rows of the first and last voxel bound the column's rows (bt is monotone in k)
     const float b_last = fmaf((float)(ZU - 1), g.dbt, g.bt0);
-    const int r0 = (int)floorf(clampf(fminf(g.bt0, b_last), -1e7f, 1e7f));
-    const int r1 = (int)floorf(clampf(fmaxf(g.bt0, b_last), -1e7f, 1e7f));
-    {
-        // a reference-valid row outside the box would be an undersized box
+    const float bmin = fminf(g.bt0, b_last), bmax = fmaxf(g.bt0, b_last);
+    g.sb = box + (uint32_t)((c - (o.y + 1) * W) * (int)sizeof(TP));  // row it (1-based) -> box row it-1-t0
+    // Every voxel's rows valid and staged: floor(bmin) >= lo + slack and floor(bmax) <= hi - slack,
+    // i.e. bmin >= lo + slack and bmax < hi + 1 - slack (integer bounds; false for NaN).  Quads hold
+    // both rows of a tap in one sample, so they need no streaming form; their fast form rounds bt to
+    // 2^-10 (twice: the column's start, then each voxel), which may reach the row next to the first
+    // or last voxel's (one row of slack each side).
+    constexpr int kSlack = kQuad<TP> ? 1 : 0;
+    if (bmin >= (float)(g.lo + kSlack) && bmax < (float)(g.hi + 1 - kSlack)) {
+        if constexpr (kQuad<TP>)
+            g.mode = 2;
+        else
+            g.mode = (g.dbt < 0.999f && g.dbt >= 0.f) ? 1 : 2;
+    } else {
+        // checked form; a reference-valid row outside the box would be an undersized box (it
+        // cannot happen in the fast forms, whose rows lie inside [lo, hi])
+        const int r0 = (int)floorf(clampf(bmin, -1e7f, 1e7f)), r1 = (int)floorf(clampf(bmax, -1e7f, 1e7f));
         const int v0 = max(1, r0), v1 = min(A.nt - 1, r1);
         if (v0 <= v1 && (v0 < g.lo || v1 > g.hi)) atomicOr(err, 1);
-    }
-    g.sb = box + (uint32_t)((c - (o.y + 1) * W) * (int)sizeof(TP));  // row it (1-based) -> box row it-1-t0
-    // quads hold both rows of a tap in one sample, so they need no streaming form; their fast
-    // form rounds bt to 2^-10 (twice: the column's start, then each voxel), which may reach the
-    // row next to the first or last voxel's (one row of slack each side)
-    if constexpr (kQuad<TP>)
-        g.mode = (r0 - 1 >= g.lo && r1 + 1 <= g.hi) ? 2 : 3;
-    else if (r0 >= g.lo && r1 <= g.hi)
-        g.mode = (g.dbt < 0.999f && g.dbt >= 0.f) ? 1 : 2;
-    else
         g.mode = 3;
+    }
     if constexpr (kQuad<TP>) {
         g.rb = (uint32_t)A.W * 8u;
         asm("cvt.rn.f16x2.f32 %0, %1, %1;" : "=r"(g.fsh) : "f"(g.fs));
