@@ -107,6 +107,19 @@ __device__ __forceinline__ void row_affine(const ViewInfo &vi, int r, int nPix, 
     *delta = (b - a) / nPix;
 }
 
+// Per (view, image row): the affine map of the row's boundaries, as the kernels use it in FP32:
+// (r0, delta, 1 / delta, |delta|), each rounded from the FP64 value.  The forward and back
+// kernels read this table instead of evaluating the FP64 map per warp: on this GPU FP64 issue is
+// narrow, and the map took most of the FP64 pipe's time.
+__global__ void bdd_rowmap_kernel(BddArgs G, const ViewInfo *info, float4 *rmap) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= (long long)G.na * G.nPix) return;
+    const int p = (int)(i / G.nPix), r = (int)(i % G.nPix);
+    double r0d, deltad;
+    row_affine(info[p], r, G.nPix, G.pSize, &r0d, &deltad);
+    rmap[i] = make_float4((float)r0d, (float)deltad, (float)(1.0 / deltad), (float)std::fabs(deltad));
+}
+
 // ------------------------------------------------------------ per-view set-up
 // forward: info, detm (nDet+1, FP32), L (nDet, FP32).  back: info and the geometry table
 // (nDet+1 float4 per view, in ascending knot order: x = knot K[j]; y = the integral of bin j per
@@ -183,7 +196,7 @@ __device__ __forceinline__ void two_sum_add(float &hi, float &lo, float v) {
 // (shuffle): neighbouring lanes read neighbouring pixels (no bank conflicts), each boundary
 // is evaluated once, and each bin is |F(k+1) - F(k)| (:98-101).
 __global__ void __launch_bounds__(kThreads)
-    bdd_project_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L,
+    bdd_project_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L, const float4 *rmap,
                        const float *__restrict__ phantom, float *sino, int rows_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet, p = blockIdx.x;
@@ -258,9 +271,8 @@ __global__ void __launch_bounds__(kThreads)
             two_sum_add(sh, sl, val[c]);
         }
         __syncwarp();
-        double r0d, deltad;
-        row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
-        const float r0 = (float)r0d, rdelta = (float)(1.0 / deltad), adelta = (float)std::fabs(deltad);
+        const float4 rmv = rmap[(size_t)p * nPix + r];
+        const float r0 = rmv.x, rdelta = rmv.z, adelta = rmv.w;
         const float qmax = (float)nPix;
         // F at mapped detector boundary k (:98, interpolation of the row's prefix integral);
         // floor(q) for 0 <= q <= nPix < 2^22 by the round-down add of 2^23 (no conversions)
@@ -311,7 +323,7 @@ static_assert(kWarps % 4 == 0, "the row maps follow the staged rows at a 16-byte
 
 template <int NG>
 __global__ void __launch_bounds__(kThreads, 4)
-    bdd_project_bins_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L,
+    bdd_project_bins_kernel(BddArgs G, const ViewInfo *info, const float *detm, const float *L, const float4 *rmap,
                             const float *__restrict__ phantom, float *sino, int rows_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet, p = blockIdx.x;
@@ -387,9 +399,8 @@ __global__ void __launch_bounds__(kThreads, 4)
                 two_sum_add(sh, sl, val[c]);
             }
             if (lane == 0) {
-                double r0d, deltad;
-                row_affine(vi, min(rb + warp, nPix - 1), nPix, G.pSize, &r0d, &deltad);
-                rm[warp] = RowMap{(float)r0d, (float)(1.0 / deltad), (float)std::fabs(deltad), 0.f};
+                const float4 rmv = rmap[(size_t)p * nPix + min(rb + warp, nPix - 1)];
+                rm[warp] = RowMap{rmv.x, rmv.z, rmv.w, 0.f};
             }
         }
         __syncthreads();
@@ -516,7 +527,8 @@ __device__ __forceinline__ int knot_search(const float4 *T, int nDet, float u) {
 // keeps that difference accurate to FP32 relative to the pixel's own integral.  Each lane owns
 // a run of consecutive pixels and walks the knots along it, reusing G at the shared boundary.
 __global__ void __launch_bounds__(kThreads)
-    bdd_back_kernel(BddArgs G, const ViewInfo *info, const float4 *tab, float *image, int views_per_cta) {
+    bdd_back_kernel(BddArgs G, const ViewInfo *info, const float4 *tab, const float4 *rmap, float *image,
+                    int views_per_cta) {
     extern __shared__ __align__(16) unsigned char smraw[];
     const int nPix = G.nPix, nDet = G.nDet;
     // per-warp pixel accumulators, skewed by one word per 16 pixels: a lane's run of pixels starts
@@ -537,9 +549,8 @@ __global__ void __launch_bounds__(kThreads)
         __syncthreads();
         if (r >= nPix) continue;
         const ViewInfo vi = info[p];
-        double r0d, deltad;
-        row_affine(vi, r, nPix, G.pSize, &r0d, &deltad);
-        const float r0 = (float)r0d, delta = (float)deltad;
+        const float4 rmv = rmap[(size_t)p * nPix + r];
+        const float r0 = rmv.x, delta = rmv.y;
         const float kfirst = T[tix(0)].x, klast = T[tix(nDet)].x;
         const int c_a = lane * per, c_b = min(nPix, c_a + per);
         if (c_a >= c_b) continue;
@@ -590,12 +601,22 @@ size_t back_smem(const BddArgs &G) {
 
 }  // namespace
 
+// Scratch layouts.  Forward: view records | detm (na x (nDet+1)) | L (na x nDet) | row maps
+// (na x nPix float4).  Back: view records | knot table | geometry table (na x (nDet+1) float4
+// each) | row maps.
+size_t proj_rowmap_offset(const BddArgs &G) {
+    return (info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + (size_t)G.na * G.nDet) + 15) / 16 * 16;
+}
+size_t back_rowmap_offset(const BddArgs &G) {
+    return info_bytes(G.na) + 2 * sizeof(float4) * (size_t)G.na * (G.nDet + 1);
+}
+
 size_t bdd_project_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + sizeof(float) * ((size_t)G.na * (G.nDet + 1) + (size_t)G.na * G.nDet);
+    return proj_rowmap_offset(G) + sizeof(float4) * (size_t)G.na * G.nPix;
 }
 
 size_t bdd_back_scratch(const BddArgs &G) {
-    return info_bytes(G.na) + 2 * sizeof(float4) * (size_t)G.na * (G.nDet + 1);  // info, knot table, geometry
+    return back_rowmap_offset(G) + sizeof(float4) * (size_t)G.na * G.nPix;
 }
 
 int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
@@ -608,7 +629,11 @@ int launch_bdd_project_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
     float *L = detm + (size_t)G.na * (G.nDet + 1);
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, detm, L,
                                                                                              nullptr);
-    return after_launch("bdd_setup_kernel");
+    SGB_TRY(after_launch("bdd_setup_kernel"));
+    float4 *rmap = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + proj_rowmap_offset(G));
+    const long long nr = (long long)G.na * G.nPix;
+    bdd_rowmap_kernel<<<(unsigned)((nr + kThreads - 1) / kThreads), kThreads, 0, st>>>(G, info, rmap);
+    return after_launch("bdd_rowmap_kernel");
 }
 
 int launch_bdd_project(const BddArgs &G, const float *phantom, float *sino, void *scratch,
@@ -627,6 +652,7 @@ int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino,
     const ViewInfo *info = static_cast<const ViewInfo *>(scratch);
     const float *detm = reinterpret_cast<const float *>(static_cast<const char *>(scratch) + info_bytes(G.na));
     const float *L = detm + (size_t)G.na * (G.nDet + 1);
+    const float4 *rmap = reinterpret_cast<const float4 *>(static_cast<const char *>(scratch) + proj_rowmap_offset(G));
     SGB_CUDA(cudaMemsetAsync(sino, 0, sizeof(float) * (size_t)G.na * G.nDet, st));
     // rows split over CTAs so that each SM holds ~8 of them (views x row blocks)
     const int target = 8 * std::max(1, num_sms());
@@ -640,15 +666,17 @@ int launch_bdd_project_main(const BddArgs &G, const float *phantom, float *sino,
         const size_t sb = project_bins_smem(G);
         if (ngroups <= kWarps * 4) {
             SGB_CUDA(cudaFuncSetAttribute(bdd_project_bins_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-            bdd_project_bins_kernel<4><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, phantom, sino, rows);
+            bdd_project_bins_kernel<4><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, rmap, phantom, sino,
+                                                                                 rows);
         } else {
             SGB_CUDA(cudaFuncSetAttribute(bdd_project_bins_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sb));
-            bdd_project_bins_kernel<8><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, phantom, sino, rows);
+            bdd_project_bins_kernel<8><<<dim3(G.na, rsplit), kThreads, sb, st>>>(G, info, detm, L, rmap, phantom, sino,
+                                                                                 rows);
         }
         return after_launch("bdd_project_bins_kernel");
     }
     SGB_CUDA(cudaFuncSetAttribute(bdd_project_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bdd_project_kernel<<<dim3(G.na, rsplit), kThreads, smem, st>>>(G, info, detm, L, phantom, sino, rows);
+    bdd_project_kernel<<<dim3(G.na, rsplit), kThreads, smem, st>>>(G, info, detm, L, rmap, phantom, sino, rows);
     return after_launch("bdd_project_kernel");
 }
 
@@ -661,7 +689,11 @@ int launch_bdd_back_setup(const BddArgs &G, void *scratch, cudaStream_t st) {
     float4 *geo = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na)) + (size_t)G.na * (G.nDet + 1);
     bdd_setup_kernel<<<dim3(G.na, (G.nDet + kSetupChunk - 1) / kSetupChunk), kThreads, 0, st>>>(G, info, nullptr, nullptr,
                                                                                              geo);
-    return after_launch("bdd_setup_kernel");
+    SGB_TRY(after_launch("bdd_setup_kernel"));
+    float4 *rmap = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + back_rowmap_offset(G));
+    const long long nr = (long long)G.na * G.nPix;
+    bdd_rowmap_kernel<<<(unsigned)((nr + kThreads - 1) / kThreads), kThreads, 0, st>>>(G, info, rmap);
+    return after_launch("bdd_rowmap_kernel");
 }
 
 int launch_bdd_back_main(const BddArgs &G, const float *sino, float *image, void *scratch, cudaStream_t st) {
@@ -673,6 +705,7 @@ int launch_bdd_back_main(const BddArgs &G, const float *sino, float *image, void
     const ViewInfo *info = static_cast<const ViewInfo *>(scratch);
     float4 *tab = reinterpret_cast<float4 *>(static_cast<char *>(scratch) + info_bytes(G.na));
     const float4 *geo = tab + (size_t)G.na * (G.nDet + 1);
+    const float4 *rmap = reinterpret_cast<const float4 *>(static_cast<const char *>(scratch) + back_rowmap_offset(G));
     SGB_CUDA(cudaMemsetAsync(image, 0, sizeof(float) * (size_t)G.nPix * G.nPix, st));
     bdd_fill_prefix_kernel<<<G.na, kThreads, 0, st>>>(G, sino, geo, tab);
     SGB_TRY(after_launch("bdd_fill_prefix_kernel"));
@@ -683,7 +716,7 @@ int launch_bdd_back_main(const BddArgs &G, const float *sino, float *image, void
     int vpc = (G.na + vsplit - 1) / vsplit;
     vsplit = (G.na + vpc - 1) / vpc;
     SGB_CUDA(cudaFuncSetAttribute(bdd_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, tab, image, vpc);
+    bdd_back_kernel<<<dim3(gx, vsplit), kThreads, smem, st>>>(G, info, tab, rmap, image, vpc);
     return after_launch("bdd_back_kernel");
 }
 
