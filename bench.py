@@ -369,6 +369,7 @@ def run_ours(args):
                 line["batched"].setdefault("forms", {})[form] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_2d:
         line["configs_2d"] = measure_2d(args)
+        line["configs_2d"]["sf_pair_arc_888x90"] = measure_sf(args)
     if ws == 1 and rank == 0 and not args.no_cpu:
         try:
             base, acc = cpu_leg({k: v.cpu().numpy() for k, v in outs.items()}, proj.cpu().numpy())
@@ -756,6 +757,65 @@ def run_dd_case(args):
                       "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
 
 
+def _sf_setup():
+    """Separable-footprint pair on the learned-filter scan geometry (SinoFanArc 888 x 90 over 360 deg,
+    512^2 at 0.9766 mm, no mask), its plan and one seeded random-ellipse phantom on the device."""
+    import torch
+
+    import sinograms as S
+    from sinograms import learned as LF
+    rg, ig = LF.sparse_fan_geometry()
+    ig = ig.with_mask(None)
+    plan = S.SFPlan(rg, ig)
+    img = LF.ellipse_image(ig, LF.phantom_ellipses(900000))
+    sino = torch.empty((rg.na, rg.nb), device="cuda")
+    back = torch.empty_like(img)
+    return rg, ig, plan, img, sino, back
+
+
+def run_sf_case(args):
+    """Separable-footprint projector pair (SinoFanArc 888 x 90, 512^2): project and back-project one
+    random-ellipse phantom through its SFPlan, 5 + 20 times each, device tensors, calls enqueued back
+    to back."""
+    rg, ig, plan, img, sino, back = _sf_setup()
+    ms = {}
+    for name, fn in (("project", lambda: plan.project(img, out=sino, sync=False)),
+                     ("backproject", lambda: plan.backproject(sino, out=back, sync=False))):
+        for _ in range(5):
+            fn()
+        ms[name] = _per_call_ms(fn, 20)
+    print(json.dumps({"case": "sf_fanarc_512x512_888x90", "ms_project": ms["project"],
+                      "ms_backproject": ms["backproject"], "sino_sum": float(sino.sum())}))
+
+
+def measure_sf(args):
+    """SF pair block of the bench line: times per call, (pixel, view) pairs per second, and the
+    accuracy of the SF and DD models against the analytic sinogram of the same phantom."""
+    import sinograms as S
+    from sinograms import learned as LF
+    reps = max(args.steps, 20)
+    out = {}
+    try:
+        rg, ig, plan, img, sino, back = _sf_setup()
+        ms_p = _per_call_ms(lambda: plan.project(img, out=sino, sync=False), reps)
+        ms_b = _per_call_ms(lambda: plan.backproject(sino, out=back, sync=False), reps)
+        pairs = float(rg.na) * ig.dims[0] * ig.dims[1]
+        ell = LF.phantom_ellipses(900000)
+        ref = S.ellipse_sino(rg, ell, device=True)
+        plan.project(img, out=sino)
+        e_sf = float(((sino - ref).pow(2).mean() / ref.pow(2).mean()).sqrt())
+        dd = LF.dd_project(img, S.BddGeo.from_geoms(rg, ig))
+        e_dd = float(((dd - ref).pow(2).mean() / ref.pow(2).mean()).sqrt())
+        out = {"ms_project": ms_p, "ms_backproject": ms_b,
+               "project_pixel_views_per_s": pairs / (ms_p / 1e3),
+               "backproject_pixel_views_per_s": pairs / (ms_b / 1e3),
+               "rel_rmse_vs_analytic_sf": e_sf, "rel_rmse_vs_analytic_dd": e_dd,
+               "call": "SFPlan calls on device tensors, enqueued back to back (one launch each)"}
+    except Exception as e:  # the headline line must still print
+        out["error"] = f"{type(e).__name__}: {e}"
+    return out
+
+
 def _lf_train_step_ms(steps):
     """Training step of the learned filter at the training script's batch: 4096 seeded rows of a
     64-scan training set of the SinoFanArc 888 x 90 workload (888 samples per row), 3 + `steps`
@@ -853,6 +913,8 @@ def run_case(args):
         return run_lf_train_case(args)
     if args.case == "lf-apply":
         return run_lf_apply_case(args)
+    if args.case == "sf-fan-888x90":
+        return run_sf_case(args)
     g = dict(GEOM, na=180)
     rg = S.CtFanFlat(**g)
     ig = S.ImageGeom((512, 512, 64), IMG["deltas"])
@@ -875,7 +937,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline / FP64 accuracy leg")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-FDK measurement")
     ap.add_argument("--no-2d", action="store_true", help="skip the 2D / learned-filter measurements")
-    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d", "lf-train", "lf-apply"],
+    ap.add_argument("--case", choices=["fdk-180v", "fdk-batch", "dd-fan-888x90", "fbp-2d", "lf-train", "lf-apply",
+                                        "sf-fan-888x90"],
                     help="run a profiling case instead")
     ap.add_argument("--storage", default="f32", choices=["f32", "bf16", "f16"], help="storage form for --case")
     args = ap.parse_args()

@@ -353,6 +353,38 @@ SGB_API double sgb_zwart_powell(double r, double phi);
 SGB_API int sgb_zwart_powell_sino(const double *r, int nr, const double *phi, int nphi, double *out, int flags,
                                   void *stream);
 
+/* _tau(rg, x, y), src/geom/tau.jl:7-60 (host, FP64): tau[i + n*v] = the projected position s/ds of
+ * the point (x[i], y[i]) in view v (the reference's length(x) x na matrix), for SGB_PAR, SGB_ARC and
+ * SGB_FLAT geometries. */
+SGB_API int sgb_tau_sino(const sgb_sino_geom *rg, const double *x, const double *y, long long n, double *tau);
+
+/* ------------------------------------------- separable-footprint projector pair */
+/* No counterpart in the reference, which sizes this system model's footprints (footprint_size,
+ * src/sys2/footprint.jl:19-36) and documents _tau as the "footprint center and support"
+ * (src/geom/tau.jl:55-57) but has no projector for it.  SF-TR model (Long, Fessler & Balter, IEEE
+ * Trans. Med. Imag. 29(11), 2010) for 2D parallel and fan beams: a pixel's footprint in bin
+ * coordinates u = tau + (nb-1)/2 + offset is the trapezoid through the projections of its four
+ * corners, scaled by its chord along the ray through its centre; a sinogram sample is the footprints'
+ * integral over its bin [k - 1/2, k + 1/2], i.e. a bin-averaged line integral (exact for parallel
+ * beams).  image (nx, ny) on a 2D ImageGeom (pixels whose mask is false are not in the model; the back
+ * projection writes 0 there), sinogram (nb, na) on an SGB_PAR / SGB_ARC / SGB_FLAT SinoGeom with d > 0.
+ * Fan beams need the whole image within 0.99 dso of the rotation centre (SGB_ERR_GEOM otherwise) and
+ * arc detectors less than +-90 degrees wide.  The back-projector is the adjoint of the projector (the
+ * same FP32 matrix elements; sums in a different order).  Both are deterministic. */
+typedef struct sgb_sf_plan sgb_sf_plan;
+SGB_API int sgb_sf_plan_create(const sgb_sino_geom *rg, const sgb_image_geom *ig, sgb_sf_plan **plan);
+/* image -> sino; flags as for the other plan calls (SGB_DEVICE_PTRS, SGB_ASYNC).  Calls on one plan
+ * share its staging buffers: serialise them on one stream. */
+SGB_API int sgb_sf_plan_project(sgb_sf_plan *plan, const float *image, float *sino, int flags, void *stream);
+/* sino -> image (the adjoint) */
+SGB_API int sgb_sf_plan_backproject(sgb_sf_plan *plan, const float *sino, float *image, int flags, void *stream);
+SGB_API int sgb_sf_plan_destroy(sgb_sf_plan *plan);
+/* One-shot forms (a plan per call; they wait for `stream` before returning, whatever the flags). */
+SGB_API int sgb_sf_project(const sgb_sino_geom *rg, const sgb_image_geom *ig, const float *image, float *sino,
+                           int flags, void *stream);
+SGB_API int sgb_sf_backproject(const sgb_sino_geom *rg, const sgb_image_geom *ig, const float *sino, float *image,
+                               int flags, void *stream);
+
 /* ------------------------------------------------------------ batched FDK */
 /* No counterpart in the reference (it reconstructs one scan per fdk call,
  * src/fbp3/fdk.jl:65-81): up to 64 independent CtFanArc/CtFanFlat scans of different sizes

@@ -686,13 +686,15 @@ void orc_ellipsoid_cone(const double *ell, int nell, int is_arc, const double *s
 
 
 /* ---------------------------------------------------------------- sys2 */
-/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-58 (always FP64, like the reference's
- * Float64 call).  BoxSp_k is written as the sum over the 2^m signed corners of the
- * active directions (the same central differences, expanded). */
+/* zwart_powell(r, z::NTuple{4}), src/sys2/zwart_powell.jl:23-26 with BoxSp0..BoxSp4 :29-58 (always
+ * FP64, like the reference's Float64 call): the Radon transform of the box spline with direction
+ * lengths z at radius r, BoxSp4 / (N-1)! with N the number of |z_k| > 1e-7.  BoxSp_k is written as
+ * the sum over the 2^m signed corners of the active directions (the same central differences,
+ * expanded). */
 static double orc_zp0(double y, int n) { return y > 0 ? pow(y, n - 1) : 0.0; }
-double orc_zwart_powell(double r, double phi) {
-    const double TOL = 1e-07, s = sin(phi), c = cos(phi);
-    const double z[4] = {c, s, c + s, c - s};
+double orc_zwart_powell_z(double r, double z1, double z2, double z3, double z4) {
+    const double TOL = 1e-07;
+    const double z[4] = {z1, z2, z3, z4};
     int n = 0;
     for (int k = 0; k < 4; k++) n += fabs(z[k]) > TOL;
     /* BoxSp4(y) = sum over sign patterns of the active z_k of (prod sign_k) y'^(N-1)_+ / prod z_k,
@@ -717,4 +719,158 @@ double orc_zwart_powell(double r, double phi) {
     double f = 1;
     for (int k = 2; k < n; k++) f *= k;
     return acc / den / f;
+}
+
+/* zwart_powell(r, phi), src/sys2/zwart_powell.jl:17-20: z = (cos, sin, cos+sin, cos-sin). */
+double orc_zwart_powell(double r, double phi) {
+    const double s = sin(phi), c = cos(phi);
+    return orc_zwart_powell_z(r, c, s, c + s, c - s);
+}
+
+/* ------------------------------------------------------- sys2: separable-footprint pair */
+/* _tau(rg, x, y), src/geom/tau.jl:7-60: the projected position s/ds of the point (x, y) in view
+ * beta.  kind 0 = SinoPar ((x cos + y sin) / ds, :8-11), 1 = SinoFanArc, 2 = SinoFanFlat (rotate,
+ * subtract the source offset, tan(gamma) = xb / (dso - yb), then dsd/ds atan(tan gamma) or
+ * dsd/ds tan gamma, :28-52). */
+static double orc_tau_point(int kind, double x, double y, double cb, double sb, double ds, double dsd,
+                            double dso, double so) {
+    if (kind == 0) return (x * cb + y * sb) / ds;
+    const double xb = x * cb + y * sb - so, yb = -x * sb + y * cb;
+    const double tg = xb / (dso - yb);
+    return kind == 1 ? dsd / ds * atan(tg) : dsd / ds * tg;
+}
+
+/* _tau(rg, x, y) for n points and na views: tau[i + n*v] (the reference's length(x) x na matrix). */
+int orc_tau(int kind, const double *betas, int na, double ds, double dsd, double dso, double so,
+            const double *x, const double *y, long n, double *tau) {
+    if (na < 0 || n < 0 || !(ds != 0)) return ORC_ERR_ARG;
+    for (int v = 0; v < na; v++) {
+        const double cb = cos(betas[v]), sb = sin(betas[v]);
+        for (long i = 0; i < n; i++) tau[i + n * v] = orc_tau_point(kind, x[i], y[i], cb, sb, ds, dsd, dso, so);
+    }
+    return ORC_OK;
+}
+
+/* Separable-footprint (SF-TR) system model for 2D parallel and fan beams: Y. Long, J. A. Fessler and
+ * J. M. Balter, "3D forward and back-projection for X-ray CT using separable footprints", IEEE Trans.
+ * Med. Imag. 29(11):1839-1850, 2010, in its 2D (transaxial) form.  The reference plans this model
+ * (src/sys2/footprint.jl sizes its footprints, and _tau in src/geom/tau.jl is documented as the
+ * "footprint center and support") but does not contain it, so this restates the published method:
+ *   - the footprint of a rectangular pixel in bin coordinates u = tau + wb (wb = (nb-1)/2 + offset,
+ *     detector bin k covering u in [k - 1/2, k + 1/2]) is the trapezoid whose vertices t0 <= t1 <=
+ *     t2 <= t3 are the projections tau of the pixel's four corners, height 1 on [t1, t2];
+ *   - its amplitude is the chord of the pixel along the ray through its centre,
+ *     h = |dx dy| / max(|dy ex|, |dx ey|) for the unit ray direction (ex, ey);
+ *   - the element of bin k is h * (G(k + 1/2) - G(k - 1/2)), G the trapezoid's integral, so a
+ *     sinogram sample is the bin-averaged line integral.
+ * For parallel beams the trapezoid times h is the exact Radon transform of the pixel, so the model
+ * is exact there.  Pixels whose mask is false are not in the model; bins outside 0..nb-1 are dropped.
+ * Image (nx, ny) and sinogram (nb, na) are column-major; the same model gives both directions. */
+static double orc_trap_cdf(double b, const double t[4]) {
+    if (b <= t[0]) return 0.0;
+    const double a01 = 0.5 * (t[1] - t[0]), a12 = t[2] - t[1], a23 = 0.5 * (t[3] - t[2]);
+    if (b <= t[1]) return (b - t[0]) * (b - t[0]) / (2 * (t[1] - t[0]));
+    if (b <= t[2]) return a01 + (b - t[1]);
+    if (b <= t[3]) return a01 + a12 + a23 - (t[3] - b) * (t[3] - b) / (2 * (t[3] - t[2]));
+    return a01 + a12 + a23;
+}
+
+static void orc_sort4(double t[4]) {
+    for (int i = 1; i < 4; i++)
+        for (int j = i; j > 0 && t[j] < t[j - 1]; j--) {
+            const double w = t[j];
+            t[j] = t[j - 1];
+            t[j - 1] = w;
+        }
+}
+
+typedef struct {
+    int kind, nb, nx, ny;
+    double ds, wb, dsd, dso, so, dx, dy, ox, oy;
+} orc_sf_geom;
+
+/* footprint of pixel (i, j) (0-based) in view beta: sorted corners t (bin coordinates), amplitude h */
+static void orc_sf_pixel(const orc_sf_geom *g, double beta, int i, int j, double t[4], double *h) {
+    const double cb = cos(beta), sb = sin(beta);
+    const double xc = g->dx * (i - ((g->nx - 1) / 2.0 + g->ox)), yc = g->dy * (j - ((g->ny - 1) / 2.0 + g->oy));
+    const double hx = 0.5 * fabs(g->dx), hy = 0.5 * fabs(g->dy);
+    for (int c = 0; c < 4; c++) {
+        const double x = xc + ((c & 1) ? hx : -hx), y = yc + ((c & 2) ? hy : -hy);
+        t[c] = orc_tau_point(g->kind, x, y, cb, sb, g->ds, g->dsd, g->dso, g->so) + g->wb;
+    }
+    orc_sort4(t);
+    double ex, ey;
+    if (g->kind == 0) {
+        ex = -sb;
+        ey = cb;
+    } else { /* from the source, rotated (source_offset, dso) */
+        const double xs = g->so * cb - g->dso * sb, ys = g->so * sb + g->dso * cb;
+        ex = xc - xs;
+        ey = yc - ys;
+        const double r = sqrt(ex * ex + ey * ey);
+        ex /= r;
+        ey /= r;
+    }
+    const double ax = fabs(g->dx), ay = fabs(g->dy);
+    *h = ax * ay / fmax(ay * fabs(ex), ax * fabs(ey));
+}
+
+static int orc_sf_check(const orc_sf_geom *g, int na) {
+    if (g->nb <= 0 || na <= 0 || g->nx <= 0 || g->ny <= 0) return ORC_ERR_ARG;
+    if (!(g->ds > 0) || !(g->dx != 0) || !(g->dy != 0)) return ORC_ERR_ARG;
+    if (g->kind != 0) { /* every pixel corner strictly in front of the source */
+        const double xm = fabs(g->dx) * (g->nx / 2.0 + fabs(g->ox)), ym = fabs(g->dy) * (g->ny / 2.0 + fabs(g->oy));
+        if (!(sqrt(xm * xm + ym * ym) < 0.99 * g->dso)) return ORC_ERR_GEOM;
+    }
+    return ORC_OK;
+}
+
+int orc_sf_project(int kind, int nb, double ds, double offset, int na, const double *betas, double dsd,
+                   double dso, double so, int nx, int ny, double dx, double dy, double ox, double oy,
+                   const uint8_t *mask, const real_t *image, real_t *sino) {
+    const orc_sf_geom g = {kind, nb, nx, ny, ds, (nb - 1) / 2.0 + offset, dsd, dso, so, dx, dy, ox, oy};
+    const int rc = orc_sf_check(&g, na);
+    if (rc) return rc;
+#pragma omp parallel for schedule(dynamic)
+    for (int v = 0; v < na; v++) {
+        double *row = (double *)calloc((size_t)nb, sizeof(double));
+        for (int j = 0; j < ny; j++)
+            for (int i = 0; i < nx; i++) {
+                const long n = i + (long)nx * j;
+                if (mask && !mask[n]) continue;
+                const double c = (double)image[n];
+                double t[4], h;
+                orc_sf_pixel(&g, betas[v], i, j, t, &h);
+                const int k0 = (int)fmax(0.0, ceil(t[0] - 0.5)), k1 = (int)fmin(nb - 1.0, floor(t[3] + 0.5));
+                for (int k = k0; k <= k1; k++)
+                    row[k] += c * h * (orc_trap_cdf(k + 0.5, t) - orc_trap_cdf(k - 0.5, t));
+            }
+        for (int k = 0; k < nb; k++) sino[k + (long)nb * v] = (real_t)row[k];
+        free(row);
+    }
+    return ORC_OK;
+}
+
+int orc_sf_back(int kind, int nb, double ds, double offset, int na, const double *betas, double dsd,
+                double dso, double so, int nx, int ny, double dx, double dy, double ox, double oy,
+                const uint8_t *mask, const real_t *sino, real_t *image) {
+    const orc_sf_geom g = {kind, nb, nx, ny, ds, (nb - 1) / 2.0 + offset, dsd, dso, so, dx, dy, ox, oy};
+    const int rc = orc_sf_check(&g, na);
+    if (rc) return rc;
+#pragma omp parallel for schedule(dynamic)
+    for (int j = 0; j < ny; j++)
+        for (int i = 0; i < nx; i++) {
+            const long n = i + (long)nx * j;
+            double acc = 0;
+            if (!mask || mask[n])
+                for (int v = 0; v < na; v++) {
+                    double t[4], h;
+                    orc_sf_pixel(&g, betas[v], i, j, t, &h);
+                    const int k0 = (int)fmax(0.0, ceil(t[0] - 0.5)), k1 = (int)fmin(nb - 1.0, floor(t[3] + 0.5));
+                    for (int k = k0; k <= k1; k++)
+                        acc += h * (orc_trap_cdf(k + 0.5, t) - orc_trap_cdf(k - 0.5, t)) * (double)sino[k + (long)nb * v];
+                }
+            image[n] = (real_t)acc;
+        }
+    return ORC_OK;
 }

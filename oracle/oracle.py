@@ -443,6 +443,69 @@ def zwart_powell(r, phi):
     return np.vectorize(lambda a, b: f(float(a), float(b)))(r, phi)
 
 
+def zwart_powell_z(r, z):
+    """zwart_powell(r, z::NTuple{4}), src/sys2/zwart_powell.jl:23-58: box-spline Radon value for
+    direction lengths z (C restatement, FP64)."""
+    f = lib(64).orc_zwart_powell_z
+    f.restype = ctypes.c_double
+    f.argtypes = [ctypes.c_double] * 5
+    z = [float(v) for v in z]
+    return np.vectorize(lambda a: f(float(a), *z))(r)
+
+
+def _kind_code(g) -> int:
+    return {"par": 0, "arc": 1, "flat": 2}[_f(g, "kind")]
+
+
+def tau(g, x, y) -> np.ndarray:
+    """_tau(rg, x, y), src/geom/tau.jl:7-60, for a 2D SinoGeom: projected s/ds of the points,
+    numpy (na, n) (the reference's n x na matrix)."""
+    x = np.ascontiguousarray(np.ravel(x), dtype=np.float64)
+    y = np.ascontiguousarray(np.ravel(y), dtype=np.float64)
+    b = ar(g)
+    out = np.zeros((len(b), len(x)))
+    _check(lib(64).orc_tau(_kind_code(g), _ptr(b), len(b), _c_double(float(_f(g, "d"))),
+                           _c_double(float(_f(g, "dsd", 0.0))), _c_double(dso(g)),
+                           _c_double(float(_f(g, "source_offset", 0.0))), _ptr(x), _ptr(y), _c_long(len(x)),
+                           _ptr(out)), "tau")
+    return out
+
+
+def _sf_args(g, ig):
+    (nx, ny), (dx, dy) = tuple(_f(ig, "dims"))[:2], tuple(_f(ig, "deltas"))[:2]
+    offs = tuple(_f(ig, "offsets", (0.0, 0.0)) or (0.0, 0.0))[:2]
+    b = ar(g)
+    return b, (_kind_code(g), int(_f(g, "nb")), _c_double(float(_f(g, "d"))),
+               _c_double(float(np.float32(_f(g, "offset", 0.0)))), len(b), _ptr(b),
+               _c_double(float(_f(g, "dsd", 0.0))), _c_double(dso(g) if _f(g, "kind") != "par" else 0.0),
+               _c_double(float(_f(g, "source_offset", 0.0))), int(nx), int(ny), _c_double(float(dx)),
+               _c_double(float(dy)), _c_double(float(offs[0])), _c_double(float(offs[1])))
+
+
+def sf_project(g, ig, image: np.ndarray, bits: int = 64) -> np.ndarray:
+    """Separable-footprint (SF-TR) projection of image (numpy (ny, nx)) -> sino (numpy (na, nb));
+    the model is stated in oracle.c (orc_sf_project)."""
+    dt = np.float64 if bits == 64 else np.float32
+    img = np.ascontiguousarray(image, dtype=dt)
+    b, args = _sf_args(g, ig)
+    out = np.zeros((len(b), int(_f(g, "nb"))), dtype=dt)
+    m = _mask(ig)
+    _check(lib(bits).orc_sf_project(*args, _ptr(m), _ptr(img), _ptr(out)), "sf_project")
+    return out
+
+
+def sf_back(g, ig, sino: np.ndarray, bits: int = 64) -> np.ndarray:
+    """Adjoint of sf_project: sino (numpy (na, nb)) -> image (numpy (ny, nx))."""
+    dt = np.float64 if bits == 64 else np.float32
+    sn = np.ascontiguousarray(sino, dtype=dt)
+    b, args = _sf_args(g, ig)
+    nx, ny = tuple(_f(ig, "dims"))[:2]
+    out = np.zeros((int(ny), int(nx)), dtype=dt)
+    m = _mask(ig)
+    _check(lib(bits).orc_sf_back(*args, _ptr(m), _ptr(sn), _ptr(out)), "sf_back")
+    return out
+
+
 def footprint_size(g, ig) -> float:
     """footprint_size(st, ig), src/sys2/footprint.jl:7-36, as Float32.  fovs(ig) =
     dims .* |deltas| (ImageGeoms 0.11)."""

@@ -13,6 +13,7 @@ from .footprint import footprint_size, zwart_powell, zwart_powell_sino
 from .geom import (CtFanArc, CtFanFlat, CtPar, CtSourceCircle, CtSourceHelix, ImageGeom, SinoFanArc, SinoFanFlat, SinoMoj, SinoPar, _ar, _d_ang, _dso, _gamma, _gamma_max, _source_dz_per_view, _source_zs, _zfov,
                    _orbit_short, _rfov, _s, _t, angles, axes, dims, downsample)
 from .phantoms import ellipse_sino, ellipsoid_proj, random_ct_scans, random_ellipses, random_ellipsoids
+from .sf import SFPlan, _tau, backproject_sf, project_sf
 from .recon import FBPNormalPlan, FDKBatch, FDKplan, cbct_back, fbp, fbp_back, fdk, plan_fbp
 
 __all__ = [n for n in dir() if not n.startswith("__")]

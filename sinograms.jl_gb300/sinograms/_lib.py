@@ -65,6 +65,13 @@ _SIGS = {
     "sgb_zwart_powell": (c_double, [c_double, c_double]),
     "sgb_zwart_powell_sino": (c_int, [P, c_int, P, c_int, P, c_int, P]),
     "sgb_selftest_wait_timeout": (c_int, [c_ll, P]),
+    "sgb_tau_sino": (c_int, [P, P, P, c_ll, P]),
+    "sgb_sf_plan_create": (c_int, [P, P, P]),
+    "sgb_sf_plan_project": (c_int, [P, P, P, c_int, P]),
+    "sgb_sf_plan_backproject": (c_int, [P, P, P, c_int, P]),
+    "sgb_sf_plan_destroy": (c_int, [P]),
+    "sgb_sf_project": (c_int, [P, P, P, P, c_int, P]),
+    "sgb_sf_backproject": (c_int, [P, P, P, P, c_int, P]),
     "sgb_fbp_sino_weight": (c_int, [P, P]),
     "sgb_fbp_sino_filter": (c_int, [P, c_int, c_ll, P, c_int, c_int, P, c_int, P]),
     "sgb_cbct_back": (c_int, [P, P, c_int, c_int, c_int, P, c_double, c_double, c_double, c_double, c_float,
