@@ -378,6 +378,11 @@ SGB_API int sgb_sf_plan_create(const sgb_sino_geom *rg, const sgb_image_geom *ig
 SGB_API int sgb_sf_plan_project(sgb_sf_plan *plan, const float *image, float *sino, int flags, void *stream);
 /* sino -> image (the adjoint) */
 SGB_API int sgb_sf_plan_backproject(sgb_sf_plan *plan, const float *sino, float *image, int flags, void *stream);
+/* The forward projector sweeps the image lines of each (view, chunk of 256 bins) in `splits` thread
+ * blocks whose partial sums are added in a fixed order (deterministic for a given value).  The plan
+ * picks it from the GPU's SM count; 1 <= splits <= 64.  Results agree to rounding. */
+SGB_API int sgb_sf_plan_set_line_splits(sgb_sf_plan *plan, int splits);
+SGB_API int sgb_sf_plan_get_line_splits(const sgb_sf_plan *plan, int *splits);
 SGB_API int sgb_sf_plan_destroy(sgb_sf_plan *plan);
 /* One-shot forms (a plan per call; they wait for `stream` before returning, whatever the flags). */
 SGB_API int sgb_sf_project(const sgb_sino_geom *rg, const sgb_image_geom *ig, const float *image, float *sino,

@@ -45,8 +45,10 @@ namespace sgb {
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
-constexpr int kFwdBins = 128;   // detector bins (threads) per forward CTA
-constexpr int kFwdCap = 256;    // footprints per line pass of a forward CTA
+constexpr int kFwdThreads = 128;                  // threads per forward CTA
+constexpr int kFwdBpt = 2;                        // adjacent detector bins per forward thread
+constexpr int kFwdBins = kFwdThreads * kFwdBpt;   // detector bins per forward CTA
+constexpr int kFwdCap = 384;                      // footprints per line pass of a forward CTA
 constexpr int kBackTx = 32, kBackTy = 8;
 constexpr int kViewChunk = 64;  // views staged in shared memory per back-projector pass
 constexpr float kRangeEps = 0.01f;  // pixel-index margin of the candidate ranges (FP32 rounding)
@@ -70,11 +72,11 @@ struct SfView {
 };
 static_assert(sizeof(SfView) == 80, "SfView layout");
 
-// Kernel arguments (FP32 image axes and index maps; f(a) = a * inv + c0 puts pixel i at [i - 1/2, i + 1/2]).
+// Kernel arguments: sizes, wb = (nb - 1)/2 + offset, the pixel's |dx|, |dy|, |dx dy| and half sizes.
 struct SfArgs {
     int nb, na, nx, ny;
+    int splits;  // forward: the image lines are split over this many CTAs per (view, chunk of bins)
     float wb, ax, ay, axy, hx, hy;
-    float xinv, xc0, yinv, yc0;
 };
 
 // One pixel's footprint in one view, relative to uc.
@@ -83,15 +85,10 @@ struct SfRec {
 };
 
 __device__ __forceinline__ float atan_small(float z) {
-    // Taylor series of atan to z^9 for |z| < 0.1 (relative error below 1e-11), else atanf.
+    // Taylor series of atan to z^5 for |z| < 0.02 (relative error below 1e-11; a pixel corner's angle
+    // from its centre seen from the source is ~1e-3), else atanf.
     const float z2 = __fmul_rn(z, z);
-    if (z2 < 0.01f) {
-        float p = __fmaf_rn(z2, 1.0f / 9.0f, -1.0f / 7.0f);
-        p = __fmaf_rn(z2, p, 1.0f / 5.0f);
-        p = __fmaf_rn(z2, p, -1.0f / 3.0f);
-        p = __fmaf_rn(z2, p, 1.0f);
-        return __fmul_rn(z, p);
-    }
+    if (z2 < 4e-4f) return __fmul_rn(z, __fmaf_rn(z2, __fmaf_rn(z2, 1.0f / 5.0f, -1.0f / 3.0f), 1.0f));
     return atanf(z);
 }
 
@@ -106,8 +103,8 @@ __host__ __device__ __forceinline__ void sf_finish(SfRec &r, float o0, float o1,
     r.d2 = fmaxf(m1, m2);
 #ifdef __CUDA_ARCH__
     const float w01 = __fsub_rn(r.d1, r.d0), w23 = __fsub_rn(r.d3, r.d2);
-    r.hr01 = w01 > 1e-20f ? __fdiv_rn(0.5f, w01) : 0.f;
-    r.hr23 = w23 > 1e-20f ? __fdiv_rn(0.5f, w23) : 0.f;
+    r.hr01 = w01 > 1e-20f ? __fdividef(0.5f, w01) : 0.f;
+    r.hr23 = w23 > 1e-20f ? __fdividef(0.5f, w23) : 0.f;
     r.c3 = __fmul_rn(0.5f, w23);
 #else
     const float w01 = r.d1 - r.d0, w23 = r.d3 - r.d2;
@@ -164,26 +161,25 @@ __device__ __forceinline__ SfRec sf_pixel(const SfView &V, const SfArgs &A, floa
     sf_finish(r, o0, o1, o2, o3);
     // chord along the ray from the source: direction (x cb + D sb, x sb - D cb), length sqrt(r2)
     const float ex = __fmaf_rn(x, V.cb, __fmul_rn(D, V.sb)), ey = __fmaf_rn(x, V.sb, -__fmul_rn(D, V.cb));
-    r.h = __fdividef(__fmul_rn(A.axy, __fsqrt_rn(r2)), fmaxf(fabsf(__fmul_rn(A.ay, ex)), fabsf(__fmul_rn(A.ax, ey))));
+    const float m = fmaxf(fabsf(__fmul_rn(A.ay, ex)), fabsf(__fmul_rn(A.ax, ey)));
+    r.h = __fdividef(A.axy, __fmul_rn(m, rsqrtf(r2)));
     return r;
 }
 
 // Pixel-index range [ia, ib] (clamped to 0..n-1) of a line whose pixels can meet the wedge between
-// two boundary rays: the rays' along-coordinates a = A + B L at the line's edges L0 and L1 bound the
-// wedge inside the line (the source lies outside the line's range, so the crossings move linearly).
-// A NaN boundary (a ray almost parallel to the lines) gives the whole line.
-__device__ __forceinline__ void sf_range(float2 lo, float2 hi, float L0, float L1, float inv, float c0, int n,
-                                         int &ia, int &ib) {
+// two boundary rays: the rays' crossings f = alpha + beta L (in pixel-index units along the line) at
+// the line's edges L0 and L1 bound the wedge inside the line (the source lies outside the line's
+// range, so the crossings move linearly).  A NaN boundary gives the whole line.
+__device__ __forceinline__ void sf_range(float2 lo, float2 hi, float L0, float L1, int n, int &ia, int &ib) {
     if (isnan(lo.x) || isnan(hi.x)) {
         ia = 0;
         ib = n - 1;
         return;
     }
-    const float a0 = __fmaf_rn(lo.y, L0, lo.x), a1 = __fmaf_rn(lo.y, L1, lo.x);
-    const float a2 = __fmaf_rn(hi.y, L0, hi.x), a3 = __fmaf_rn(hi.y, L1, hi.x);
-    const float f0 = __fmaf_rn(fminf(fminf(a0, a1), fminf(a2, a3)), inv, c0);
-    const float f1 = __fmaf_rn(fmaxf(fmaxf(a0, a1), fmaxf(a2, a3)), inv, c0);
-    const float fl = fminf(f0, f1) + (0.5f - kRangeEps), fh = fmaxf(f0, f1) + (0.5f + kRangeEps);
+    const float f0 = __fmaf_rn(lo.y, L0, lo.x), f1 = __fmaf_rn(lo.y, L1, lo.x);
+    const float f2 = __fmaf_rn(hi.y, L0, hi.x), f3 = __fmaf_rn(hi.y, L1, hi.x);
+    const float fl = fminf(fminf(f0, f1), fminf(f2, f3)) + (0.5f - kRangeEps);
+    const float fh = fmaxf(fmaxf(f0, f1), fmaxf(f2, f3)) + (0.5f + kRangeEps);
     ia = max(0, (int)floorf(fminf(fmaxf(fl, -1.f), (float)n)));
     ib = min(n - 1, (int)floorf(fminf(fmaxf(fh, -1.f), (float)n)));
 }
@@ -229,7 +225,9 @@ __global__ void sf_setup_views(SfGeo G, const double *betas, SfView *views) {
 }
 
 // Boundary rays: for boundary j (u = j - 1/2, j = 0..nb) the along-coordinate of its crossing with
-// the line at line-coordinate L is A + B L (rows: x at y = L; columns: y at x = L).  A fan ray that
+// the line at line-coordinate L is A + B L (rows: x at y = L; columns: y at x = L); the table holds it
+// in pixel-index units, alpha + beta L with alpha = A / d + c0 and beta = B / d for the along axis's
+// pixel size d and centre index c0.  A fan ray that
 // does not point toward the lines (the source lies on one side of all of them), or is within 1e-6 of
 // parallel to them, is stored as NaN: a wedge bounded by such a ray may contain the direction
 // parallel to the lines, where crossings run off to infinity, so its range is the whole line.  Ray
@@ -258,49 +256,52 @@ __global__ void sf_setup_rays(SfGeo G, const double *betas, const SfView *views,
         const double toward = rows ? (ys > G.yhi ? -dyr : dyr) : (xs > G.xhi ? -dxr : dxr);
         if (!(toward > 1e-6)) B = HUGE_VAL;
     }
+    const double d = rows ? G.dx : G.dy, c0 = rows ? (G.nx - 1) / 2.0 + G.ox : (G.ny - 1) / 2.0 + G.oy;
     float2 out;
     if (!(fabs(B) <= 1e6)) out = make_float2(nanf(""), nanf(""));
-    else out = make_float2((float)A, (float)B);
+    else out = make_float2((float)(A / d + c0), (float)(B / d));
     rays[i] = out;
 }
 
 // ------------------------------------------------------------------- forward
 template <int GEO>
-__global__ void __launch_bounds__(kFwdBins) sf_project_kernel(SfArgs A, const SfView *__restrict__ views,
-                                                              const float2 *__restrict__ rays,
-                                                              const float *__restrict__ xcs,
-                                                              const float *__restrict__ ycs,
-                                                              const float *__restrict__ image,
-                                                              const uint8_t *__restrict__ mask,
-                                                              float *__restrict__ sino) {
+__global__ void __launch_bounds__(kFwdThreads) sf_project_kernel(SfArgs A, const SfView *__restrict__ views,
+                                                                 const float2 *__restrict__ rays,
+                                                                 const float *__restrict__ xcs,
+                                                                 const float *__restrict__ ycs,
+                                                                 const float *__restrict__ image,
+                                                                 const uint8_t *__restrict__ mask,
+                                                                 float *__restrict__ sino) {
     __shared__ float4 s0[2][kFwdCap];  // uc, d0, d1, d2
     __shared__ float4 s1[2][kFwdCap];  // d3, hr01, hr23, c3 (fan beams)
     __shared__ float2 s2[2][kFwdCap];  // h, pixel value
     const int v = blockIdx.y, tid = threadIdx.x;
-    const int k0 = blockIdx.x * kFwdBins, kend = min(k0 + kFwdBins, A.nb), k = k0 + tid;
+    const int k0 = blockIdx.x * kFwdBins, kend = min(k0 + kFwdBins, A.nb);
+    const int ka = k0 + kFwdBpt * tid, kb = min(ka + kFwdBpt, A.nb);  // this thread's bins [ka, kb)
     const SfView V = views[v];
     const bool rows = V.rows != 0;
     const int nal = rows ? A.nx : A.ny, nln = rows ? A.ny : A.nx;
     const float *lcs = rows ? ycs : xcs;
-    const float ainv = rows ? A.xinv : A.yinv, ac0 = rows ? A.xc0 : A.yc0;
     const float hl = rows ? A.hy : A.hx;
     const float2 *R = rays + (size_t)v * (A.nb + 1);
     const float2 cl = R[k0], ch = R[kend];
-    const bool active = k < A.nb;
-    const float2 bl = R[min(k, A.nb)], bh = R[min(k + 1, A.nb)];
-    const float klo = (float)k - 0.5f, khi = (float)k + 0.5f;
-    float acc = 0.f;
+    const bool active = ka < A.nb;
+    const float2 bl = R[min(ka, A.nb)], bh = R[max(kb, 0)];
+    // boundaries of bins ka and ka + 1 (exact in FP32, as the back-projector forms them)
+    const float e0 = (float)ka - 0.5f, e1 = (float)ka + 0.5f, e2 = (float)(ka + 1) + 0.5f;
+    const int per = (nln + A.splits - 1) / A.splits, jb = blockIdx.z * per, je = min(nln, jb + per);
+    float acc0 = 0.f, acc1 = 0.f;
     int buf = 0;
-    for (int j = 0; j < nln; j++) {
+    for (int j = jb; j < je; j++) {
         const float lc = lcs[j], L0 = lc - hl, L1 = lc + hl;
         int ia, ib;
-        sf_range(cl, ch, L0, L1, ainv, ac0, nal, ia, ib);
+        sf_range(cl, ch, L0, L1, nal, ia, ib);
         if (ia > ib) continue;  // same for the whole CTA
         int qa = 0, qb = -1;
-        if (active) sf_range(bl, bh, L0, L1, ainv, ac0, nal, qa, qb);
+        if (active) sf_range(bl, bh, L0, L1, nal, qa, qb);
         for (int p0 = ia; p0 <= ib; p0 += kFwdCap) {
             const int p1 = min(ib, p0 + kFwdCap - 1);
-            for (int t = tid; t <= p1 - p0; t += kFwdBins) {
+            for (int t = tid; t <= p1 - p0; t += kFwdThreads) {
                 const int i = p0 + t;
                 const int px = rows ? i : j, py = rows ? j : i;
                 const size_t n = (size_t)px + (size_t)A.nx * py;
@@ -337,13 +338,26 @@ __global__ void __launch_bounds__(kFwdBins) sf_project_kernel(SfArgs A, const Sf
                     r.hr23 = a1.z;
                     r.c3 = a1.w;
                 }
-                const float g = __fsub_rn(sf_cdf(__fsub_rn(khi, r.uc), r), sf_cdf(__fsub_rn(klo, r.uc), r));
-                acc = __fmaf_rn(__fmul_rn(a2.x, g), a2.y, acc);
+                const float g0 = sf_cdf(__fsub_rn(e0, r.uc), r), g1 = sf_cdf(__fsub_rn(e1, r.uc), r);
+                const float g2 = sf_cdf(__fsub_rn(e2, r.uc), r);
+                acc0 = __fmaf_rn(__fmul_rn(a2.x, __fsub_rn(g1, g0)), a2.y, acc0);
+                acc1 = __fmaf_rn(__fmul_rn(a2.x, __fsub_rn(g2, g1)), a2.y, acc1);
             }
             buf ^= 1;
         }
     }
-    if (active) sino[(size_t)k + (size_t)A.nb * v] = acc;
+    // splits > 1: partial sums, added in split order by sf_sum_splits
+    float *row = sino + (size_t)A.nb * (v + (size_t)A.na * blockIdx.z);
+    if (active) row[ka] = acc0;
+    if (ka + 1 < A.nb) row[ka + 1] = acc1;
+}
+
+__global__ void sf_sum_splits(const float *__restrict__ part, int splits, long long n, float *__restrict__ sino) {
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float s = part[i];
+    for (int z = 1; z < splits; z++) s = __fadd_rn(s, part[i + n * z]);
+    sino[i] = s;
 }
 
 // ------------------------------------------------------------------- back
@@ -399,7 +413,7 @@ using namespace sgb;
 struct sgb_sf_plan {
     SfGeo G{};
     SfArgs A{};
-    DevBuf betas, views, rays, axes, mask, din, dout;
+    DevBuf betas, views, rays, axes, mask, din, dout, part;
     const uint8_t *mask_dev = nullptr;
 };
 
@@ -454,6 +468,20 @@ int sf_geometry(const sgb_sino_geom *rg, const sgb_image_geom *ig, SfGeo *G) {
     return SGB_OK;
 }
 
+// Line splits of the forward projector: enough CTAs for about two resident waves of four-warp
+// CTAs (16 per SM), at most 16 and at least 8 image lines per CTA.
+int sf_default_splits(const SfGeo &G) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaGetLastError();
+    const long long ctas = (long long)((G.nb + kFwdBins - 1) / kFwdBins) * G.na;
+    const long long want = 2LL * 16 * std::max(sms, 1);
+    int s = (int)std::min<long long>(16, std::max<long long>(1, (want + ctas - 1) / ctas));
+    const int lines = std::max(G.nx, G.ny);
+    while (s > 1 && lines / s < 8) s--;
+    return s;
+}
+
 int sf_run(sgb_sf_plan *P, bool forward, const float *in, float *out, int flags, cudaStream_t st) {
     const SfGeo &G = P->G;
     const size_t nimg = (size_t)G.nx * G.ny, nsino = (size_t)G.nb * G.na;
@@ -469,15 +497,26 @@ int sf_run(sgb_sf_plan *P, bool forward, const float *in, float *out, int flags,
     const SfView *views = P->views.as<SfView>();
     const float *src = static_cast<const float *>(in_dev);
     if (forward) {
-        const dim3 grid((G.nb + kFwdBins - 1) / kFwdBins, G.na);
+        const int splits = P->A.splits;
+        const dim3 grid((G.nb + kFwdBins - 1) / kFwdBins, G.na, splits);
+        static_assert(kFwdBpt == 2, "sf_project_kernel accumulates two bins per thread");
         const float2 *rays = P->rays.as<float2>();
+        float *dst = out_dev;
+        if (splits > 1) {
+            SGB_TRY(P->part.reserve(sizeof(float) * nsino * splits));
+            dst = P->part.as<float>();
+        }
         if (G.kind == SGB_PAR)
-            sf_project_kernel<0><<<grid, kFwdBins, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, out_dev);
+            sf_project_kernel<0><<<grid, kFwdThreads, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, dst);
         else if (G.kind == SGB_ARC)
-            sf_project_kernel<1><<<grid, kFwdBins, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, out_dev);
+            sf_project_kernel<1><<<grid, kFwdThreads, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, dst);
         else
-            sf_project_kernel<2><<<grid, kFwdBins, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, out_dev);
+            sf_project_kernel<2><<<grid, kFwdThreads, 0, st>>>(P->A, views, rays, xcs, ycs, src, P->mask_dev, dst);
         SGB_TRY(after_launch("sf_project_kernel"));
+        if (splits > 1) {
+            sf_sum_splits<<<(unsigned)((nsino + 255) / 256), 256, 0, st>>>(dst, splits, (long long)nsino, out_dev);
+            SGB_TRY(after_launch("sf_sum_splits"));
+        }
     } else {
         const dim3 grid((G.nx + kBackTx - 1) / kBackTx, (G.ny + kBackTy - 1) / kBackTy), block(kBackTx, kBackTy);
         if (G.kind == SGB_PAR)
@@ -535,10 +574,7 @@ int sgb_sf_plan_create(const sgb_sino_geom *rg, const sgb_image_geom *ig, sgb_sf
     A.axy = (float)std::fabs(G.dx * G.dy);
     A.hx = (float)(0.5 * std::fabs(G.dx));
     A.hy = (float)(0.5 * std::fabs(G.dy));
-    A.xinv = (float)(1.0 / G.dx);
-    A.xc0 = (float)((G.nx - 1) / 2.0 + G.ox);
-    A.yinv = (float)(1.0 / G.dy);
-    A.yc0 = (float)((G.ny - 1) / 2.0 + G.oy);
+    A.splits = sf_default_splits(G);
     SGB_TRY(P->views.reserve(sizeof(SfView) * G.na));
     SGB_TRY(P->rays.reserve(sizeof(float2) * (size_t)G.na * (G.nb + 1)));
     sf_setup_views<<<(G.na + 127) / 128, 128, 0, st>>>(G, P->betas.as<double>(), P->views.as<SfView>());
@@ -560,6 +596,18 @@ int sgb_sf_plan_project(sgb_sf_plan *P, const float *image, float *sino, int fla
 int sgb_sf_plan_backproject(sgb_sf_plan *P, const float *sino, float *image, int flags, void *stream) {
     SGB_REQUIRE(P && sino && image, "sf_plan_backproject: null argument");
     return sf_run(P, false, sino, image, flags, static_cast<cudaStream_t>(stream));
+}
+
+int sgb_sf_plan_set_line_splits(sgb_sf_plan *P, int splits) {
+    SGB_REQUIRE(P && splits >= 1 && splits <= 64, "sf_plan_set_line_splits: need 1 <= splits <= 64");
+    P->A.splits = splits;
+    return SGB_OK;
+}
+
+int sgb_sf_plan_get_line_splits(const sgb_sf_plan *P, int *splits) {
+    SGB_REQUIRE(P && splits, "sf_plan_get_line_splits: null argument");
+    *splits = P->A.splits;
+    return SGB_OK;
 }
 
 int sgb_sf_plan_destroy(sgb_sf_plan *P) {

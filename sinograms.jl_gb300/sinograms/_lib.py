@@ -70,6 +70,8 @@ _SIGS = {
     "sgb_sf_plan_project": (c_int, [P, P, P, c_int, P]),
     "sgb_sf_plan_backproject": (c_int, [P, P, P, c_int, P]),
     "sgb_sf_plan_destroy": (c_int, [P]),
+    "sgb_sf_plan_set_line_splits": (c_int, [P, c_int]),
+    "sgb_sf_plan_get_line_splits": (c_int, [P, P]),
     "sgb_sf_project": (c_int, [P, P, P, P, c_int, P]),
     "sgb_sf_backproject": (c_int, [P, P, P, P, c_int, P]),
     "sgb_fbp_sino_weight": (c_int, [P, P]),

@@ -66,6 +66,17 @@ class SFPlan:
             _lib.lib().sgb_sf_plan_destroy(h)
             self._h = None
 
+    @property
+    def line_splits(self) -> int:
+        """Thread blocks the forward projector splits each (view, bin chunk)'s image lines over."""
+        v = ctypes.c_int()
+        _check(_lib.lib().sgb_sf_plan_get_line_splits(self._h, ctypes.byref(v)), "sf_plan_get_line_splits")
+        return v.value
+
+    @line_splits.setter
+    def line_splits(self, n: int) -> None:
+        _check(_lib.lib().sgb_sf_plan_set_line_splits(self._h, int(n)), "sf_plan_set_line_splits")
+
     def _call(self, fn, x, in_shape, out_shape, out, sync):
         a = Arr(x)
         if tuple(a.shape) != in_shape:

@@ -129,6 +129,24 @@ def test_sf_is_deterministic_and_paths_agree(cuda):
     np.testing.assert_array_equal(b, plan.backproject(torch.from_numpy(a).to(cuda)).cpu().numpy())
 
 
+@pytest.mark.parametrize("splits", [1, 2, 3, 8, 64])
+def test_sf_forward_line_splits(cuda, splits):
+    """Any split of the image lines over thread blocks gives the oracle's projection; each split
+    count is deterministic."""
+    for name in ("arc", "flat-wide", "par-180-neg-dy"):
+        g, ig = CASES[name]
+        nx, ny = ig["dims"]
+        img = np.random.default_rng(12).random((ny, nx)).astype(np.float32)
+        plan = S.SFPlan(C.to_geom(g), C.to_image(ig))
+        plan.line_splits = splits
+        assert plan.line_splits == splits
+        a = plan.project(img)
+        close(a, O.sf_project(g, ig, img))
+        np.testing.assert_array_equal(a, plan.project(img))
+    with pytest.raises(S.SinogramsArgumentError):
+        plan.line_splits = 0
+
+
 def test_sf_parallel_single_pixels_are_box_splines(cuda):
     """SinoPar on the GPU: one pixel's projection is the bin-integrated Radon transform of the
     rectangle, zwart_powell(k - uc, (dx cos/ds, dy sin/ds, 1, 0)) dx dy / ds (zwart_powell.jl:23-58)."""
