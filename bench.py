@@ -281,6 +281,7 @@ def run_ours(args):
     # streams, as a scan-after-scan user would run them, so one step's copies overlap the
     # other's back-projection; the wall clock spans all steps and the final synchronisation.
     plans = [forms[head]["plan"], S.plan_fbp(rg, ig, storage=head)]
+    plans[0].set_timing(False)  # a user's call: no stage-timing events
     streams = [torch.cuda.Stream(), torch.cuda.Stream()]
     hproj = torch.empty(proj.shape, dtype=torch.float32, pin_memory=True)
     hproj.copy_(proj)

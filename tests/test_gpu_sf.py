@@ -188,6 +188,39 @@ def test_sf_edge_cases(cuda, case):
     close(_run(g, ig, sino, False), O.sf_back(g, ig, sino))
 
 
+@pytest.mark.parametrize("kind", ["par", "arc", "flat"])
+@pytest.mark.parametrize("scale", ["fine-pixels", "fine-bins"])
+def test_sf_extreme_pixel_to_bin_ratios(cuda, kind, scale):
+    """fine-pixels: 0.25 mm pixels under 4 mm bins, so a 256-bin chunk of the forward projector sees
+    more footprints per image line than one shared-memory pass holds (several passes per line);
+    fine-bins: 4 mm pixels over 0.1 mm bins, so every footprint spans tens of bins."""
+    if scale == "fine-pixels":
+        g = geom(kind, nb=300, d=4.0, offset=0.5, na=12)
+        ig = dict(dims=(1024, 48), deltas=(0.25, 0.3), offsets=(0.0, 3.0))
+    else:
+        g = geom(kind, nb=900, d=0.1, offset=-0.5, na=12)
+        ig = dict(dims=(20, 18), deltas=(4.0, 3.5), offsets=(0.25, 0.0))
+    if kind != "par":
+        g.update(dsd=900.0, dod=400.0)
+    nx, ny = ig["dims"]
+    rng = np.random.default_rng(21)
+    img = rng.random((ny, nx))
+    sino = rng.random((g["na"], g["nb"]))
+    for splits in (1, 3):
+        plan = S.SFPlan(C.to_geom(g), C.to_image(ig))
+        plan.line_splits = splits
+        close(plan.project(img.astype(np.float32)), O.sf_project(g, ig, img))
+    close(_run(g, ig, sino, False), O.sf_back(g, ig, sino))
+
+
+def test_sf_large_image_matches_oracle(cuda):
+    """A 1024^2 image at 0.5 mm under the 888-bin flat detector, 60 views."""
+    g = dict(ARC888, kind="flat", na=60, orbit_start=3.0, offset=-0.75)
+    ig = dict(dims=(1024, 1024), deltas=(0.5, 0.5), offsets=(0.0, 0.0))
+    img = np.random.default_rng(22).random((1024, 1024))
+    close(_run(g, ig, img, True), O.sf_project(g, ig, img))
+
+
 def test_sf_and_dd_agree_with_the_analytic_sinogram(cuda):
     """On the 888 x 90 arc scan (centred detector, as the distance-driven pair has no offset) both
     system models approach the analytic line integrals of an ellipse phantom; SF is the closer one."""
