@@ -153,8 +153,10 @@ int plan_common(sgb_plan *P, int kind, int ndet, double d, double dsd, const sgb
     }
     std::vector<double> g;
     spatial_kernel(P->Hk, g);
-    // three BF16 pieces (FP32-class rows); two when the filtered rows are stored in BF16
-    SGB_TRY(P->filt.build(g, ndet, (ndet + 7) / 8 * 8, P->storage == SGB_STORE_BF16 ? 2 : 3, st));
+    // three BF16 pieces (FP32-class rows, ~4e-8); two (~7e-6) when the FDK plan stores the filtered
+    // rows in BF16 or FP16 quads, whose own rounding (2^-8, 2^-11) is far coarser
+    const bool reduced = P->storage == SGB_STORE_BF16 || (P->ct && P->storage == SGB_STORE_F16);
+    SGB_TRY(P->filt.build(g, ndet, (ndet + 7) / 8 * 8, reduced ? 2 : 3, st));
     SGB_TRY(P->flags.reserve(4 * sizeof(int)));
     SGB_CUDA(cudaMemsetAsync(P->flags.p, 0, 4 * sizeof(int), st));
     P->filt_err = P->flags.as<int>() + 3;
