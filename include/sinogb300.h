@@ -363,7 +363,7 @@ SGB_API int sgb_tau_sino(const sgb_sino_geom *rg, const double *x, const double 
 /* ------------------------------------------- separable-footprint projector pair */
 /* No counterpart in the reference, which sizes this system model's footprints (footprint_size,
  * src/sys2/footprint.jl:19-36) and documents _tau as the "footprint center and support"
- * (src/geom/tau.jl:55-57) but has no projector for it.  SF-TR model (Long, Fessler & Balter, IEEE
+ * (src/geom/tau.jl:57-60) but has no projector for it.  SF-TR model (Long, Fessler & Balter, IEEE
  * Trans. Med. Imag. 29(11), 2010) for 2D parallel and fan beams: a pixel's footprint in bin
  * coordinates u = tau + (nb-1)/2 + offset is the trapezoid through the projections of its four
  * corners, scaled by its chord along the ray through its centre; a sinogram sample is the footprints'

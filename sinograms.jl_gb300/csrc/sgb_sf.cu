@@ -3,7 +3,7 @@
 //
 // No counterpart in the reference, which plans this system model (footprint_size in
 // src/sys2/footprint.jl:19-36 sizes its footprints, and _tau is documented as the "footprint
-// center and support", tau.jl:55-57) but does not contain it.  The model is the SF-TR method of
+// center and support", tau.jl:57-60) but does not contain it.  The model is the SF-TR method of
 // Y. Long, J. A. Fessler and J. M. Balter (IEEE Trans. Med. Imag. 29(11):1839-1850, 2010) in its
 // 2D (transaxial) form:
 //   * bin coordinate u = tau + wb, wb = (nb - 1)/2 + offset; detector bin k covers [k - 1/2, k + 1/2];

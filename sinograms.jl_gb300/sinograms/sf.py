@@ -30,7 +30,7 @@ def _tau(rg, x, y) -> np.ndarray:
         raise SinogramsArgumentError("_tau here takes a 2D SinoGeom")
     x, y = f64(np.ravel(x)), f64(np.ravel(y))
     if x.shape != y.shape:
-        raise SinogramsArgumentError("x,y axes")  # tau.jl:42
+        raise SinogramsArgumentError("x,y axes")  # tau.jl:44
     out = np.zeros((int(rg.na), len(x)))
     _lib.check(_lib.lib().sgb_tau_sino(ctypes.byref(c_struct(rg)), ptr(x), ptr(y), len(x), ptr(out)), "tau")
     return out
