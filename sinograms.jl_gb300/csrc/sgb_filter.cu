@@ -176,36 +176,53 @@ __device__ __forceinline__ float bf16_hi(uint32_t u) { return __uint_as_float(u 
 // Weighted first differences of every row, split into NP BF16 pieces:
 // D[p][row][k] for k < kpad (zero for k >= ns).  One thread per 4 samples of a row.
 template <int NP>
+__device__ __forceinline__ void split_group(const FilterArgs &A, __nv_bfloat16 *__restrict__ D, long long row, int k0,
+                                            int t, int a, long long pstride) {
+    const Five x = load5(A.in + row * A.ns, 1, k0, A.ns, 0.f);
+    const Five wa = load5(A.wA ? A.wA + (long long)a * A.sAa : nullptr, A.sAj, k0, A.ns, 1.f);
+    const Five wb = load5(A.wB ? A.wB + (long long)t * A.sBt : nullptr, A.sBj, k0, A.ns, 1.f);
+    // weights in the order of the reference's broadcast: p * A * B * scale
+    float v[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) v[i] = x.v[i] * wa.v[i] * wb.v[i] * A.scale;
+    const float prev = x.p * wa.p * wb.p * A.scale;
+    float d[4] = {v[0] - prev, v[1] - v[0], v[2] - v[1], v[3] - v[2]};
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+        if (k0 + i >= A.ns) d[i] = 0.f;
+    __nv_bfloat16 *dst = D + row * A.kpad + k0;
+#pragma unroll
+    for (int p = 0; p < NP; p++) {
+        const uint32_t lo = pack_bf16(d[0], d[1]), hi = pack_bf16(d[2], d[3]);
+        *reinterpret_cast<uint2 *>(dst + p * pstride) = make_uint2(lo, hi);
+        d[0] -= bf16_lo(lo);
+        d[1] -= bf16_hi(lo);
+        d[2] -= bf16_lo(hi);
+        d[3] -= bf16_hi(hi);
+    }
+}
+
+template <int NP>
 __global__ void __launch_bounds__(256) split_rows_kernel(const FilterArgs A, __nv_bfloat16 *__restrict__ D) {
     const int ng = A.kpad >> 2;
     const long long total = A.nrows * ng, pstride = A.nrows * (long long)A.kpad;
+    if (total <= 0x7fffffffLL) {
+        // 32-bit index arithmetic: three 64-bit divisions per group cost more issue slots than the
+        // group's memory traffic
+        const unsigned ung = (unsigned)ng, unt = (unsigned)A.nt, una = (unsigned)A.na, utot = (unsigned)total;
+        const unsigned step = gridDim.x * blockDim.x;
+        for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < utot; idx += step) {
+            const unsigned row = idx / ung;
+            split_group<NP>(A, D, row, (int)(idx - row * ung) << 2, (int)(row % unt), (int)((row / unt) % una),
+                            pstride);
+        }
+        return;
+    }
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < total;
          idx += (long long)gridDim.x * blockDim.x) {
         const long long row = idx / ng;
-        const int k0 = (int)(idx - row * ng) << 2;
-        const int t = (int)(row % A.nt), a = (int)((row / A.nt) % A.na);
-        const Five x = load5(A.in + row * A.ns, 1, k0, A.ns, 0.f);
-        const Five wa = load5(A.wA ? A.wA + (long long)a * A.sAa : nullptr, A.sAj, k0, A.ns, 1.f);
-        const Five wb = load5(A.wB ? A.wB + (long long)t * A.sBt : nullptr, A.sBj, k0, A.ns, 1.f);
-        // weights in the order of the reference's broadcast: p * A * B * scale
-        float v[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) v[i] = x.v[i] * wa.v[i] * wb.v[i] * A.scale;
-        const float prev = x.p * wa.p * wb.p * A.scale;
-        float d[4] = {v[0] - prev, v[1] - v[0], v[2] - v[1], v[3] - v[2]};
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-            if (k0 + i >= A.ns) d[i] = 0.f;
-        __nv_bfloat16 *dst = D + row * A.kpad + k0;
-#pragma unroll
-        for (int p = 0; p < NP; p++) {
-            const uint32_t lo = pack_bf16(d[0], d[1]), hi = pack_bf16(d[2], d[3]);
-            *reinterpret_cast<uint2 *>(dst + p * pstride) = make_uint2(lo, hi);
-            d[0] -= bf16_lo(lo);
-            d[1] -= bf16_hi(lo);
-            d[2] -= bf16_lo(hi);
-            d[3] -= bf16_hi(hi);
-        }
+        split_group<NP>(A, D, row, (int)(idx - row * ng) << 2, (int)(row % A.nt), (int)((row / A.nt) % A.na),
+                        pstride);
     }
 }
 
