@@ -581,7 +581,7 @@ int sgb_plan_last_timing(sgb_plan *P, double *ms, int n) {
 }
 
 static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *out, cudaStream_t st,
-                      int nout = 0) {
+                      int nout = 0, unsigned *amax = nullptr) {
     FilterArgs A{};
     A.in = in_dev;
     A.ns = P->ndet;
@@ -596,6 +596,7 @@ static int run_filter(sgb_plan *P, const float *in_dev, long long nrows, void *o
     A.sBj = P->sBj;
     A.sBt = P->sBt;
     A.scale = P->scale;
+    A.amax = amax;
     A.err = P->filt_err;
     // FP32 pairs for the pair boxes; F16 plans filter to FP32 rows that become quads afterwards
     const bool pairs = P->ct && P->tma && P->targs.elem_bytes == 8 && !P->targs.quad;
@@ -609,9 +610,12 @@ static int filter_projections(sgb_plan *P, const float *in_dev, cudaStream_t st)
     const sgb_ct_geom &g = P->cg;
     const long long rows = (long long)g.nt * g.na;
     if (!(P->tma && P->targs.quad)) return run_filter(P, in_dev, rows, P->filt_buf.p, st, P->pitch);
-    SGB_TRY(run_filter(P, in_dev, rows, P->qtmp.p, st, P->pitch));
-    return launch_quad_pack(P->qtmp.as<float>(), P->pitch, g.ns, g.nt, rows, P->filt_buf.p, P->qword.as<unsigned>(),
-                            P->qword.as<float>() + 1, st);
+    // the filter's epilogue folds max |y| into the quads' scale word as it stores the FP32 rows
+    unsigned *amax = P->qword.as<unsigned>();
+    SGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+    SGB_TRY(run_filter(P, in_dev, rows, P->qtmp.p, st, P->pitch, amax));
+    return launch_quad_pack(P->qtmp.as<float>(), P->pitch, g.ns, g.nt, rows, P->filt_buf.p, amax,
+                            P->qword.as<float>() + 1, st, true);
 }
 
 int sgb_fdk(sgb_plan *P, const float *proj, float *image, int flags, void *stream) {

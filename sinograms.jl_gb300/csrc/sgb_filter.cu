@@ -439,6 +439,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int c0 = ((warp - 2) >> 2) * kEpiCols;
         using TE = typename OutElem<TO>::T;
         TE *out = static_cast<TE *>(A.out);
+        float vmax = 0.f;  // max |y| of the stored FP32 rows (A.amax)
         uint32_t j = 0;
         for (long long tile = t_first; tile < ntiles; tile += t_step, j++) {
             const uint32_t buf = j % C::kBufs, use = j / C::kBufs;
@@ -481,12 +482,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                     if (row < A.nrows) store_pairs32(orow + cc, v, next, ncols - cc, A.nout - 1 - (n0 + cc), A.ovec);
                 } else if (row < A.nrows) {
                     store_row32<TO>(orow + cc, v, ncols - cc, A.ovec);
+                    if constexpr (std::is_same<TO, float>::value)
+                        if (A.amax)
+#pragma unroll
+                            for (int i = 0; i < 32; i++)
+                                if (i < ncols - cc) vmax = fmaxf(vmax, fabsf(v[i]));
                 }
             }
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0) mbar_arrive(accempty + buf);
         }
+        if constexpr (std::is_same<TO, float>::value)
+            if (A.amax) {
+                const unsigned w = __reduce_max_sync(0xffffffffu, __float_as_uint(vmax));
+                if (lane == 0 && w) atomicMax(A.amax, w);
+            }
     }
 
     __syncwarp();
@@ -506,6 +517,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int r0 = rank * kM / ksplit, r1 = min((rank + 1) * kM / ksplit, (int)(A.nrows - m0 < kM ? A.nrows - m0 : kM));
         using TE = typename OutElem<TO>::T;
         TE *out = static_cast<TE *>(A.out);
+        float vmax = 0.f;
         for (int idx = threadIdx.x; idx < (r1 - r0) * nc4; idx += kThreads) {
             const int r = r0 + idx / nc4, c = 4 * (idx % nc4);
             const float *src = reinterpret_cast<const float *>(smem) + r * kPartStride + c;
@@ -532,9 +544,15 @@ __global__ void __launch_bounds__(kThreads, 1)
                     dst[i] = make_float2(v[i], d);
                 } else {
                     store_one(dst + i, v[i]);
+                    vmax = fmaxf(vmax, fabsf(v[i]));
                 }
             }
         }
+        if constexpr (std::is_same<TO, float>::value)
+            if (A.amax) {
+                const unsigned w = __reduce_max_sync(0xffffffffu, __float_as_uint(vmax));
+                if ((threadIdx.x & 31) == 0 && w) atomicMax(A.amax, w);
+            }
         cl.sync();  // peers' partials stay in place until every rank has read them
     }
 }

@@ -21,6 +21,7 @@ struct FilterArgs {
     const float *wB;     // B[j*sBj + t*sBt] or null
     long long sBj, sBt;
     float scale;         // scalar weight (dbeta)
+    unsigned *amax;      // FP32 rows only, optional: atomicMax of max |y| (bits of a non-negative float)
     // set by launch_filter_rows
     void *out;
     int kpad, nblk;      // K padded to the stage width; 256-column output blocks
@@ -56,9 +57,10 @@ int launch_filter_rows(const FilterArgs &A, const FilterOperator &F, DevBuf &scr
 
 // F16 storage form of FDK: FP32 filtered rows y (nrows = nt * na rows of `pitch` samples, ns of
 // data) -> FP16 quads (8 bytes per sample, same layout), scaled by a power of two from max|y|;
-// *unscale receives the inverse scale (device word).  `amax` is a device word of scratch.
+// *unscale receives the inverse scale (device word).  `amax` is a device word of scratch; with
+// amax_ready it already holds max |y| (the filter's epilogue folded it in) and no max pass runs.
 int launch_quad_pack(const float *y, int pitch, int ns, int nt, long long nrows, void *quads, unsigned *amax,
-                     float *unscale, cudaStream_t st);
+                     float *unscale, cudaStream_t st, bool amax_ready = false);
 
 // cuTensorMapEncodeTiled from the driver entry-point table (null when unavailable)
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn();

@@ -85,19 +85,23 @@ __global__ void __launch_bounds__(256) quad_pack_kernel(const float *__restrict_
 
 }  // namespace
 
+// amax_ready: the filter's epilogue has already folded max |y| of these rows into *amax (zeroed
+// before the filter ran), so the separate max pass is skipped.
 int launch_quad_pack(const float *y, int pitch, int ns, int nt, long long nrows, void *quads, unsigned *amax,
-                     float *unscale, cudaStream_t st) {
+                     float *unscale, cudaStream_t st, bool amax_ready) {
     SGB_REQUIRE(pitch % 4 == 0 && pitch >= ns && nt >= 1 && nrows % nt == 0, "quad_pack: bad layout");
     SGB_REQUIRE(reinterpret_cast<uintptr_t>(y) % 16 == 0 && reinterpret_cast<uintptr_t>(quads) % 16 == 0,
                 "quad_pack: buffers must be 16-byte aligned");
     if (nrows <= 0) return SGB_OK;
-    SGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
     const long long n4 = nrows * (pitch / 4);
-    const int sms = num_sms();
-    SGB_REQUIRE(sms > 0, "quad_pack: no CUDA device");
-    const unsigned mblocks = (unsigned)std::min<long long>((n4 + 255) / 256, (long long)sms * 8);
-    absmax_kernel<<<mblocks, 256, 0, st>>>(reinterpret_cast<const float4 *>(y), n4, amax);
-    SGB_TRY(after_launch("absmax_kernel"));
+    if (!amax_ready) {
+        SGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned), st));
+        const int sms = num_sms();
+        SGB_REQUIRE(sms > 0, "quad_pack: no CUDA device");
+        const unsigned mblocks = (unsigned)std::min<long long>((n4 + 255) / 256, (long long)sms * 8);
+        absmax_kernel<<<mblocks, 256, 0, st>>>(reinterpret_cast<const float4 *>(y), n4, amax);
+        SGB_TRY(after_launch("absmax_kernel"));
+    }
     quad_pack_kernel<<<(unsigned)((n4 + 255) / 256), 256, 0, st>>>(y, pitch, ns, nt, nrows, amax,
                                                                    static_cast<uint4 *>(quads), unscale);
     return after_launch("quad_pack_kernel");
