@@ -236,3 +236,44 @@ def test_sf_and_dd_agree_with_the_analytic_sinogram(cuda):
     e_dd = O.rel_rmse(dd, ref)
     assert e_sf < 1e-2, (e_sf, e_dd)
     assert e_sf < e_dd, (e_sf, e_dd)
+
+
+def _random_case(seed):
+    """A seeded random geometry inside the pair's limits: the image within 0.99 dso, arc detectors
+    narrower than +-90 degrees."""
+    rng = np.random.default_rng(1000 + seed)
+    kind = ("par", "arc", "flat")[seed % 3]
+    nx, ny = int(rng.integers(1, 48)), int(rng.integers(1, 48))
+    dx, dy = float(rng.uniform(0.3, 2.5)), float(rng.uniform(0.3, 2.5)) * (1 if rng.random() < 0.8 else -1)
+    ig = dict(dims=(nx, ny), deltas=(dx, dy), offsets=(float(rng.uniform(-2, 2)), float(rng.uniform(-2, 2))))
+    g = dict(kind=kind, nb=int(rng.integers(1, 160)), d=float(rng.uniform(0.2, 3.0)),
+             offset=float(np.float32(rng.uniform(-3, 3))), na=int(rng.integers(1, 40)),
+             orbit=float(rng.choice([180.0, 360.0, 217.5])), orbit_start=float(rng.uniform(-90, 90)))
+    if kind != "par":
+        rmax = np.hypot(abs(dx) * (nx / 2 + 2), abs(dy) * (ny / 2 + 2))
+        dso = float(rmax / 0.9 + rng.uniform(5, 300))
+        dsd = dso + float(rng.uniform(10, 400))
+        # keep the arc detector inside +-80 degrees
+        if kind == "arc":
+            g["nb"] = min(g["nb"], int(2 * 1.39 * dsd / g["d"]) - 2)
+        g.update(dsd=dsd, dod=dsd - dso, source_offset=float(rng.uniform(-3, 3)))
+    return g, ig
+
+
+@pytest.mark.parametrize("seed", range(18))
+def test_sf_random_geometries(cuda, seed):
+    g, ig = _random_case(seed)
+    nx, ny = ig["dims"]
+    rng = np.random.default_rng(seed)
+    img = rng.random((ny, nx))
+    sino = rng.random((g["na"], g["nb"]))
+    ref_p = O.sf_project(g, ig, img)
+    ref_b = O.sf_back(g, ig, sino)
+    if np.abs(ref_p).max() > 0:  # the image may miss a narrow detector entirely
+        close(_run(g, ig, img, True), ref_p)
+    else:
+        assert np.abs(_run(g, ig, img, True)).max() == 0
+    if np.abs(ref_b).max() > 0:
+        close(_run(g, ig, sino, False), ref_b)
+    else:
+        assert np.abs(_run(g, ig, sino, False)).max() == 0
