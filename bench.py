@@ -828,7 +828,14 @@ def measure_sf(args):
                "project_pixel_views_per_s": pairs / (ms_p / 1e3),
                "backproject_pixel_views_per_s": pairs / (ms_b / 1e3),
                "rel_rmse_vs_analytic_sf": e_sf, "rel_rmse_vs_analytic_dd": e_dd,
-               "call": "SFPlan calls on device tensors, enqueued back to back (one launch each)"}
+               "call": "SFPlan calls on device tensors, enqueued back to back (one launch each)",
+               # both kernels are bound by instruction issue (ncu issue-active of each, one launch)
+               "roofline": {"bound": "issue",
+                            "project_issue_active": _from_profile("sf_kernels_fanarc888_90v.md",
+                                                                  "sf_project_issue_active"),
+                            "backproject_issue_active": _from_profile("sf_kernels_fanarc888_90v.md",
+                                                                      "sf_back_issue_active"),
+                            "source": "profiles/sf_kernels_fanarc888_90v.md (ncu smsp__issue_active)"}}
     except Exception as e:  # the headline line must still print
         out["error"] = f"{type(e).__name__}: {e}"
     return out
