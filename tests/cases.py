@@ -47,6 +47,11 @@ ARC_SHORT = dict(rg=short(_ARC, 48), ig=PAR["ig"], window="none")
 FLAT = dict(rg=dict(_ARC, kind="flat"), ig=PAR["ig"], window="hamming")
 BDD = dict(DSD=300.0, DS0=180.0, pSize=2.0, dSize=2.3, nPix=32, nDet=40, angle=np.arange(24) * (2 * math.pi / 24))
 FILTER_WRAP = dict(nb=24, npad=32, extra=3, rows=5)
+# separable-footprint pair: rectangular pixels, detector and image offsets, a source offset for the fans
+SF_IG = dict(dims=(24, 20), deltas=(1.2, 0.9), offsets=(0.5, -0.75))
+SF = {kind: dict(rg=dict(kind=kind, nb=40, d=1.1, offset=0.25, na=16, orbit=360.0, orbit_start=10.0,
+                         **({} if kind == "par" else dict(dsd=200.0, dod=90.0, source_offset=0.8))), ig=SF_IG)
+      for kind in ("par", "arc", "flat")}
 # 3D parallel beam (CtPar, type3.jl:102-115): 200 degrees so the Parker ramp of SinoPar applies
 CT_PAR = dict(rg=dict(kind="par", ns=40, nt=24, ds=1.0, dt=1.2, offset_s=0.25, offset_t=-0.5, na=40, orbit=200.0,
                       orbit_start=10.0),

@@ -1,6 +1,7 @@
 """Generate the committed golden fixtures (small .npz files) from the FP64 oracle.
 
-Run from the repository root:  python tests/golden/make_fixtures.py
+Run from the repository root:  python tests/golden/make_fixtures.py [name ...]
+(no names: every fixture; names: only those, e.g. `sf`, leaving the others' files untouched)
 Each fixture stores the FP32 input the GPU receives and the FP64 oracle output for a
 geometry defined in tests/cases.py.  The oracle itself is pinned by tests/test_oracle.py
 against the reference's known answers and conservation tests
@@ -42,7 +43,19 @@ def main():
     ph = rng.random((g["nPix"], g["nPix"])).astype(np.float32)
     y = rng.random((g["nDet"], len(g["angle"]))).astype(np.float32)
     out["bdd"] = dict(phantom=ph, sino=y, ref_proj=O.project_bdd(ph, geo), ref_back=O.backproject_bdd(y, geo))
+    sf = {}
+    rs = np.random.default_rng(11)
+    for kind, c in C.SF.items():
+        nx, ny = c["ig"]["dims"]
+        img = rs.random((ny, nx)).astype(np.float32)
+        sn = rs.random((c["rg"]["na"], c["rg"]["nb"])).astype(np.float32)
+        sf.update({f"{kind}_image": img, f"{kind}_sino": sn, f"{kind}_ref_proj": O.sf_project(c["rg"], c["ig"], img),
+                   f"{kind}_ref_back": O.sf_back(c["rg"], c["ig"], sn)})
+    out["sf"] = sf
+    wanted = set(sys.argv[1:])
     for name, d in out.items():
+        if wanted and name not in wanted:
+            continue
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **d)
         print("wrote", name)
 

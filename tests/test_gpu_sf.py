@@ -72,6 +72,16 @@ def test_sf_pair_matches_oracle(cuda, name):
 
 
 @pytest.mark.parametrize("kind", ["par", "arc", "flat"])
+def test_sf_golden_fixtures(cuda, kind):
+    """The committed FP64 fixtures (tests/golden/sf.npz) for the three geometries."""
+    import os
+    f = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sf.npz"))
+    c = C.SF[kind]
+    close(_run(c["rg"], c["ig"], f[f"{kind}_image"], True), f[f"{kind}_ref_proj"])
+    close(_run(c["rg"], c["ig"], f[f"{kind}_sino"], False), f[f"{kind}_ref_back"])
+
+
+@pytest.mark.parametrize("kind", ["par", "arc", "flat"])
 def test_sf_masked_image(cuda, kind):
     g, ig = CASES[kind]
     nx, ny = ig["dims"]

@@ -159,3 +159,15 @@ def test_sf_geometry_errors_without_gpu():
         S.SFPlan(S.SinoPar(nb=64, na=8), S.ImageGeom((8, 8, 4), (1.0, 1.0, 1.0)))
     with pytest.raises(S.SinogramsArgumentError):
         S.SFPlan(S.SinoMoj(nb=64, na=8), ig)
+
+
+@pytest.mark.parametrize("kind", KINDS)
+def test_sf_fixture_reproduces(kind):
+    """tests/golden/sf.npz (made by make_fixtures.py from the FP64 oracle) is what the oracle computes."""
+    import os
+    f = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "sf.npz"))
+    c = C.SF[kind]
+    np.testing.assert_allclose(O.sf_project(c["rg"], c["ig"], f[f"{kind}_image"]), f[f"{kind}_ref_proj"], rtol=1e-12,
+                               atol=1e-12)
+    np.testing.assert_allclose(O.sf_back(c["rg"], c["ig"], f[f"{kind}_sino"]), f[f"{kind}_ref_back"], rtol=1e-12,
+                               atol=1e-12)
